@@ -1,0 +1,421 @@
+"""Benchmark: pair-interactions/s of the Lennard-Jones MD step on GB300.
+
+Workload (the dense-liquid mixed-precision configuration): N = 16384
+particles, periodic box at rho* = 0.85, T* = 1.0, FCC lattice with seeded
++-0.02 sigma jitter, Maxwell velocities, dt = 0.005, TVN constant-kinetic-
+temperature dynamics, no cutoff (all N(N-1) ordered pairs per step, the
+count the reference kernel evaluates).  A step is one full Verlet+TVN step
+(drift, all-pairs forces, reductions, thermostat, observables).
+
+Prints one JSON line (rank 0):
+  value       pair-interactions/s of the mixed FP32/FP64 path, inputs resident
+              in HBM, device-timed per step with CUDA events, L2 flushed
+              between timed steps;
+  e2e         the same metric through the public C ABI with host buffers:
+              every step uploads positions+velocities from pinned host memory,
+              steps, and reads positions+velocities+observables back;
+  fp64        the all-FP64 GPU path on the same box (the 3x comparator);
+  accuracy    per-particle force error of the mixed path vs FP64;
+  roofline    pair kernel vs the FP32 peak (38 flops per ordered pair);
+  cpu_baseline the reference's CPU algorithm (float-storage restatement of
+              MDSystem.cpp's CPU path) on the host cores, a bounded sample.
+
+--impl reference times that CPU implementation alone on the same workload.
+Multi-GPU (torchrun): every rank runs an independent replica (the path has
+no data exchange between boxes), value = total over ranks, scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "lennard-jones-cuda_gb300"), os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+N = 16384
+RHO = 0.85
+T0 = 1.0
+DT = 0.005
+JITTER = 0.02
+SEED = 2
+FLOPS_PER_PAIR = 38  # FMA = 2, rcp = 1 (roofline numerator)
+WORKLOAD = "lj-dense-liquid-tvn N=16384 rho*=0.85 T*=1.0 FCC+0.02 dt=0.005"
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the reference's CPU algorithm (faithful float-storage restatement)
+# ---------------------------------------------------------------------------
+def cpu_state():
+    import ljgb
+    cfg = ljgb.config(n=N, temperature=T0, density=RHO, canonical=1, lattice=ljgb.LATTICE_FCC, jitter=JITTER,
+                      seed=SEED)
+    pos, vel = ljgb.sample_initial_state(cfg)
+    L = (N / RHO) ** (1.0 / 3.0)
+    p4 = np.zeros((N, 4), np.float32)
+    p4[:, :3] = pos
+    p4[:, 3] = np.float32(L / 150.0)
+    v4 = np.zeros((N, 4), np.float32)
+    v4[:, :3] = vel
+    return p4, v4
+
+
+def cpu_baseline(max_seconds=12.0, max_steps=None, threads=None):
+    """Times MDSystem.cpp's CPU Integrate (restated in oracle/lj_oracle.c,
+    parallel over i) on this host: full N=16384 TVN steps until max_seconds."""
+    import oracle
+    oracle.build()
+    threads = threads or oracle.default_threads()
+    p4, v4 = cpu_state()
+    r = oracle.R32System(N, T0, RHO, True, 0, p4, v4)
+    r.calculate_forces(threads)
+    r.calculate_parameters()
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        r.integrate(DT, threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= max_seconds or (max_steps and steps >= max_steps):
+            break
+    rate = N * (N - 1) * steps / el
+    return {"value": rate, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
+            "sample": "%d full TVN steps of the N=16384 workload (%.1f s), reference CPU algorithm "
+                      "(float storage, MDSystem.cpp:237-583) restated in C, OpenMP over i" % (steps, el),
+            "seconds": el, "steps": steps}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def make_system(ljgb, prec, device):
+    return ljgb.System(n=N, density=RHO, temperature=T0, canonical=1, lattice=ljgb.LATTICE_FCC, jitter=JITTER,
+                       seed=SEED, precision=prec, device=device)
+
+
+def timed_steps(torch, s, steps, warmup, flush):
+    """Per-step CUDA-event timing on the library's stream, L2 flushed before
+    every timed step (flush writes a buffer larger than L2)."""
+    ext = torch.cuda.ExternalStream(s.stream())
+    for _ in range(warmup):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        s.integrate(DT)
+    s.sync()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    c0 = s.launch_count()
+    for k in range(steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            starts[k].record(ext)
+        s.integrate(DT)
+        with torch.cuda.stream(ext):
+            ends[k].record(ext)
+    s.sync()
+    launches = s.launch_count() - c0
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    return sum(ms), ms, launches
+
+
+def e2e_steps(ljgb, s, steps, warmup):
+    """Through the public API with host buffers: per step upload pos+vel from
+    pinned memory, one step, download pos+vel and the observables."""
+    pos = ljgb.pinned((N, 3))
+    vel = ljgb.pinned((N, 3))
+    s.get_state_into(pos, vel, None)
+    for _ in range(warmup):
+        s.set_state_from(pos, vel)
+        s.integrate(DT)
+        s.get_state_into(pos, vel, None)
+        s.observables()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.set_state_from(pos, vel)
+        s.integrate(DT)
+        s.get_state_into(pos, vel, None)
+        s.observables()
+    el = time.perf_counter() - t0
+    obs_bytes = 14 * 8
+    return el, {"h2d_bytes_per_step": 2 * N * 3 * 8, "d2h_bytes_per_step": 2 * N * 3 * 8 + obs_bytes}
+
+
+def fp32_peak_nominal(device):
+    """SMs x 128 FP32 lanes x 2 flops x maximum SM clock."""
+    import torch
+    props = torch.cuda.get_device_properties(device)
+    mhz = None
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", str(device), "--query-gpu=clocks.max.sm",
+                              "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=20)
+        mhz = float(out.stdout.strip().splitlines()[0])
+    except Exception:
+        mhz = 2070.0
+    return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12, props.multi_processor_count, mhz
+
+
+def read_traffic():
+    """Per-launch DRAM bytes of the pair kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "pairs_mixed_n16384_ncu.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def accuracy(ljgb, oracle, device):
+    """Mixed vs FP64 forces on the benchmark state: all particles vs the GPU
+    FP64 path, and 512 seeded rows vs the CPU FP64 oracle."""
+    a = make_system(ljgb, 0, device)
+    b = make_system(ljgb, 1, device)
+    pos, _, Fa = a.get_state()
+    _, _, Fb = b.get_state()
+    ea, _ = a.pair_sums()
+    oa, ob = a.observables(), b.observables()
+    d = np.linalg.norm(Fa - Fb, axis=1)
+    mag = np.linalg.norm(Fb, axis=1)
+    rms = float(np.sqrt(np.mean(mag ** 2)))
+    rel = d / mag
+    rows = (4096, 4608)
+    r = oracle.f64_forces(pos, a.L, True, rows=rows)
+    dc = np.linalg.norm(Fa[rows[0]:rows[1]] - r["F"], axis=1)
+    out = {
+        "vs": "all-FP64 GPU path (all N) and FP64 CPU oracle (512 rows)",
+        "force_rel_median": float(np.median(rel)), "force_rel_p99": float(np.percentile(rel, 99)),
+        "force_rel_max": float(rel.max()), "force_rms_rel_max": float(d.max() / rms),
+        "oracle_rms_rel_max": float(dc.max() / rms),
+        "V_rel": abs(oa["V"] - ob["V"]) / abs(ob["V"]), "W_rel": abs(oa["W"] - ob["W"]) / abs(ob["W"]),
+        "gate": "max |dF_i|/rms|F| <= 1e-5 and p99 |dF_i|/|F_i| <= 1e-5",
+    }
+    out["gate_pass"] = bool(out["force_rms_rel_max"] <= 1e-5 and out["force_rel_p99"] <= 1e-5
+                            and out["oracle_rms_rel_max"] <= 1e-5)
+    a.close()
+    b.close()
+    return out
+
+
+def gpu_arm(args, rank, world, local_rank):
+    import torch
+    import ljgb
+    import oracle
+    ljgb.load()
+    oracle.build()
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    s = make_system(ljgb, 0, dev)
+    s.autotune()
+    tune = s.tune_info()
+    shape = tune["shapes"][tune["active"]]
+
+    dist = world > 1
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        total_ms, per_step, launches = timed_steps(torch, s, args.steps, args.warmup, flush)
+    torch.cuda.synchronize()
+    if dist:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    pairs_step = N * (N - 1)
+    value = world * pairs_step * args.steps / (total_ms * 1e-3)
+    ms_step = total_ms / args.steps
+
+    # pair-kernel duration inside the same step graph (event nodes around it)
+    s.profile(True)
+    ext = torch.cuda.ExternalStream(s.stream())
+    for _ in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        s.integrate(DT)
+    prof = s.profile_read()
+    s.profile(False)
+    pair_ms = prof["pair_ms"] / max(1, prof["pair_launches"])
+    step_ms_prof = prof["step_ms"] / max(1, prof["steps"])
+
+    # e2e through the C ABI with host buffers
+    e2e_s, e2e_bytes = e2e_steps(ljgb, s, args.steps, args.warmup)
+    e2e_value = world * pairs_step * args.steps / e2e_s
+    s.close()
+
+    result = None
+    if rank == 0:
+        # FP64 comparator (same workload, fewer steps)
+        f = make_system(ljgb, 1, dev)
+        k64 = max(3, min(args.steps, 20))
+        ms64, _, _ = timed_steps(torch, f, k64, 2, flush)
+        f.close()
+        fp64_value = pairs_step * k64 / (ms64 * 1e-3)
+        acc = accuracy(ljgb, oracle, dev)
+        peak, sms, mhz = fp32_peak_nominal(dev)
+        achieved = FLOPS_PER_PAIR * pairs_step / (pair_ms * 1e-3) / 1e12
+        traffic = read_traffic()
+        cpu = cpu_baseline(max_seconds=args.cpu_seconds)
+        result = {
+            "metric": "pair-interactions/s, N=16384, FP32-mixed vs FP64 same GB300 @ force rel err<=1e-5",
+            "value": value, "unit": "pair-interactions/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-pairs/f64-state", "data": "synthetic (seeded FCC+jitter, Maxwell)",
+            "config": {"workload": WORKLOAD, "n": N, "rho": RHO, "T": T0, "dt": DT, "ensemble": "TVN",
+                       "parallelism": "replicas" if world > 1 else "single", "l2": "flushed (256 MB write) "
+                       "before every timed step", "kernel_shape": shape},
+            "steps_per_s": 1e3 / ms_step,
+            "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step":
+                    e2e_bytes["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e_bytes["d2h_bytes_per_step"],
+                    "ms_per_step": e2e_s * 1e3 / args.steps},
+            "fp64": {"value": fp64_value, "unit": "pair-interactions/s", "ms_per_step": ms64 / k64, "steps": k64,
+                     "mixed_over_fp64": value / world / fp64_value},
+            "accuracy": acc,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_pairs_mixed", "flops_per_pair": FLOPS_PER_PAIR,
+                         "pair_kernel_ms": pair_ms, "step_ms_profiled": step_ms_prof,
+                         "step_frac": FLOPS_PER_PAIR * pairs_step / (ms_step * 1e-3) / 1e12 / peak,
+                         "peak_source": "nominal FP32: %d SMs x 128 lanes x 2 x %.0f MHz (MEASURED_PEAKS.json "
+                                        "has no FP32 figure)" % (sms, mhz)},
+            "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+    return result
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    # Each "step" is one full N=16384 TVN step of the reference CPU algorithm;
+    # the run is capped so that warm-up + steps stay within a few minutes.
+    import oracle
+    oracle.build()
+    threads = oracle.default_threads()
+    p4, v4 = cpu_state()
+    r = oracle.R32System(N, T0, RHO, True, 0, p4, v4)
+    r.calculate_forces(threads)
+    r.calculate_parameters()
+    t0 = time.perf_counter()
+    r.integrate(DT, threads)
+    one = time.perf_counter() - t0
+    budget = 150.0
+    steps = max(1, min(args.steps, int(budget / max(one, 1e-3)) - 1))
+    for _ in range(max(0, min(args.warmup, 1) - 1)):
+        r.integrate(DT, threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r.integrate(DT, threads)
+    el = time.perf_counter() - t0
+    value = N * (N - 1) * steps / el
+    return {
+        "metric": "pair-interactions/s, N=16384, FP32-mixed vs FP64 same GB300 @ force rel err<=1e-5",
+        "impl": "reference", "value": value, "unit": "pair-interactions/s", "n_gpus": world, "steps": steps,
+        "warmup": 1, "ms_per_step": el * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-storage/f64-temporaries", "data": "synthetic (seeded FCC+jitter)",
+        "config": {"workload": WORKLOAD, "n": N, "rho": RHO, "T": T0, "dt": DT, "ensemble": "TVN"},
+        "cpu_baseline": {"value": value, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
+                         "sample": "%d full TVN steps of the N=16384 workload; MDSystem.cpp CPU path restated "
+                                   "bit-exactly in C (oracle/lj_oracle.c), OpenMP over i" % steps},
+        "e2e": {"value": value, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own sources are not present on this machine; the bit-exact C restatement of "
+                "its CPU path runs instead (pinned to the reference by tests/golden)",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        res = reference_arm(args, rank, world)
+    else:
+        if world > 1:
+            import torch
+            torch.cuda.set_device(local_rank)
+            torch.distributed.init_process_group("nccl")
+        res = gpu_arm(args, rank, world, local_rank)
+        if world > 1:
+            import torch
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,261 @@
+/*
+ * lj_gb300.h -- C ABI of the GB300-native Lennard-Jones MD hot path.
+ *
+ * One handle (lj_system) owns one simulation box on one GPU: FP64 positions
+ * and velocities resident in HBM, the FP32/fixed-point shadow the pair
+ * kernel reads, forces, observables and the step graphs.  Every entry point
+ * returns an lj_status (0 = LJ_OK) and never exits the process; the message
+ * of the last failure on a handle is available from lj_last_error().
+ *
+ * It replaces, in the reference (vlvovch/lennard-jones-cuda):
+ *   - the host integrator and observables of class MDSystem
+ *     (src/library/MDSystem.cpp:325-359 CalculateParameters,
+ *      :406-436 ApplyBoundaryConditions, :438-583 Integrate),
+ *   - the CUDA force path behind the extern "C" block of
+ *     src/library/MDSystem.cu:155-299 (calculateNForces, allocate/copy),
+ *     whose exact signatures are kept separately in lj_reference_abi.h,
+ *   - the RDF and velocity histograms (MDSystem.cpp:93-97, 633-694).
+ * Each declaration cites the reference interface it stands in for.
+ *
+ * Units are reduced LJ units (m = 1); epsilon and sigma default to 1, the
+ * reference's hard-coded values (MDSystem.cu:44-53, MDSystem.cpp:289-298).
+ * Arrays are interleaved (x, y, z) per particle, N x 3 doubles.
+ */
+#ifndef LJ_GB300_H
+#define LJ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Opaque handle: one box (or a batch of boxes) resident on one GPU. */
+typedef struct lj_system lj_system;
+
+typedef enum {
+  LJ_OK = 0,
+  LJ_ERR_INVALID = 1,     /* bad argument (null pointer, N < 2, rho <= 0, ...) */
+  LJ_ERR_CUDA = 2,        /* a CUDA runtime call failed (message holds the CUDA error) */
+  LJ_ERR_NO_DEVICE = 3,   /* no usable sm_103 device, or the kernels were not built for it */
+  LJ_ERR_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up; results of that launch are void */
+  LJ_ERR_NONFINITE = 5,   /* an observable became NaN/Inf (overlapping particles, blow-up) */
+  LJ_ERR_UNSUPPORTED = 6, /* requested mode is not provided (e.g. the CPU hardware mode) */
+  LJ_ERR_OUT_OF_MEMORY = 7
+} lj_status;
+
+/* Boundary conditions, MDSystem.h:24: 0 periodic, 1 hard wall, 2 none. */
+enum { LJ_BC_PERIODIC = 0, LJ_BC_WALL = 1, LJ_BC_NONE = 2 };
+
+/* Arithmetic of the pair loop.  MIXED: fixed-point positions, FP32 pair math
+ * with compensated per-particle sums, FP64 positions/velocities/reductions.
+ * FP64: every pair computed in double (the all-FP64 comparator path). */
+enum { LJ_PREC_MIXED = 0, LJ_PREC_FP64 = 1 };
+
+/* Initial lattice: SC is the reference's cell-centred simple-cubic lattice
+ * (MDSystem.cpp:150-167); FCC fills ceil((N/4)^(1/3))^3 cells in lattice order. */
+enum { LJ_LATTICE_SC = 0, LJ_LATTICE_FCC = 1 };
+
+/* RDF bin layouts.  R2_CLAMP: the reference GPU rule, bins in r^2 with the
+ * overflow counted in the last bin (MDSystem.cu:39).  R2_DROP: the reference
+ * CPU rule, overflow dropped (MDSystem.cpp:282-284).  R_LINEAR: bins linear
+ * in r up to rmax, pairs beyond rmax dropped. */
+enum { LJ_RDF_R2_CLAMP = 0, LJ_RDF_R2_DROP = 1, LJ_RDF_R_LINEAR = 2 };
+
+/* MDSystem::MDSystemConfiguration (MDSystem.h:10-41) plus the parameters the
+ * reference hard-codes or seeds from the clock. */
+typedef struct {
+  int32_t n;            /* N, number of particles (MDSystem.h:12) */
+  double temperature;   /* T0 (MDSystem.h:15) */
+  double density;       /* rho (MDSystem.h:18); box side L = (N/rho)^(1/3) */
+  int32_t canonical;    /* 0 EVN velocity Verlet, 1 TVN (MDSystem.h:21) */
+  int32_t boundary;     /* LJ_BC_* (MDSystem.h:25) */
+  int32_t precision;    /* LJ_PREC_* */
+  double epsilon;       /* LJ energy scale, 1 in the reference */
+  double sigma;         /* LJ length scale, 1 in the reference */
+  int32_t lattice;      /* LJ_LATTICE_* */
+  double jitter;        /* uniform displacement half-width in sigma, 0 = none */
+  uint64_t seed;        /* seed of the initial-condition generator */
+  int32_t block_hint;   /* CUDABlockSize (MDSystem.h:29); 0 = use the autotuned shape */
+  int32_t device;       /* CUDA device ordinal */
+  int32_t autotune;     /* 1: time the kernel shapes on first use and keep the fastest */
+} lj_config;
+
+/* Thermodynamic state after the last force evaluation / step.  Same
+ * definitions as MDSystem::CalculateParameters (MDSystem.cpp:325-359):
+ * K = sum v^2/2, V = 4 eps sum_{i<j}[(s/r)^12-(s/r)^6], T = 2K/(3N),
+ * P = (W/6 + N T)/(N/rho) with W = sum over ordered pairs of r.f, U = K + V. */
+typedef struct {
+  double t;          /* simulation time (MDSystem.h:80) */
+  double K, V, T, P, U;
+  double W;          /* virial sum over ordered pairs, r_ij . f_ij */
+  double Pshear;     /* off-diagonal stress (0 unless shear accumulation is enabled) */
+  double Tkin_tvn;   /* TVN: kinetic temperature of the half-kicked velocities, else 0 */
+  double av_U_tot, av_T_tot, av_p_tot; /* running sums, MDSystem.h:98 */
+  int64_t av_iters;  /* MDSystem.h:99 */
+  int64_t step;      /* steps taken since creation */
+} lj_observables;
+
+/* Fills *cfg with MDSystemConfiguration's defaults (MDSystem.h:32-40):
+ * N=128, T0=1.5, rho=0.2, EVN, periodic; plus eps=sigma=1, SC lattice,
+ * no jitter, seed 1, mixed precision, device 0, autotune on. */
+lj_status lj_config_default(lj_config* cfg);
+
+/* MDSystem::MDSystem / Reinitialize (MDSystem.cpp:55-114): allocates the box
+ * on cfg->device, samples the seeded initial state (lattice, jitter, Maxwell
+ * speeds, zero momentum, exact-T0 rescale), computes forces and observables
+ * and resets the running averages. */
+lj_status lj_create(const lj_config* cfg, lj_system** out);
+
+/* MDSystem::~MDSystem (MDSystem.cpp:218-230), without the process-wide
+ * device reset the reference performs through threadExit(). */
+lj_status lj_destroy(lj_system* sys);
+
+/* Message of the last failed call on sys (or of the last failed lj_create
+ * when sys is NULL).  Valid until the next call on the same handle. */
+const char* lj_last_error(const lj_system* sys);
+
+/* Box side L and particle count. */
+lj_status lj_get_info(const lj_system* sys, int32_t* n, double* box);
+
+/* Reinitialize with a new configuration on the same handle
+ * (MDSystem::Reinitialize, MDSystem.cpp:66-114). */
+lj_status lj_reinitialize(lj_system* sys, const lj_config* cfg);
+
+/* Inject positions/velocities (N x 3 doubles, either may be NULL) -- the
+ * reference's writes into h_Pos/h_Vel followed by setArray (MDSystem.cpp:615-630).
+ * Forces are NOT recomputed; call lj_compute_forces. */
+lj_status lj_set_state(lj_system* sys, const double* pos, const double* vel);
+
+/* Read back state (N x 3 doubles each, any may be NULL) -- getArray(0/1)
+ * (MDSystem.cpp:586-613) and h_Force. */
+lj_status lj_get_state(lj_system* sys, double* pos, double* vel, double* force);
+
+/* Per-particle pair sums of the last force evaluation, N doubles each (any
+ * may be NULL): e_i = sum_j 4eps[(s/r)^12-(s/r)^6] (the reference's Force.w
+ * times 4 eps), w_i = sum_j r_ij.f_ij. */
+lj_status lj_get_pair_sums(lj_system* sys, double* e, double* w);
+
+/* MDSystem::CalculateForces + CalculateParameters (MDSystem.cpp:232-359):
+ * forces, V, virial at the current positions, then K, T, P, U; the running
+ * averages advance by one sample like CalculateParameters does. */
+lj_status lj_compute_forces(lj_system* sys);
+
+/* MDSystem::Integrate(dt) nsteps times (MDSystem.cpp:438-583): velocity
+ * Verlet (EVN) or constant-kinetic-temperature Verlet (TVN), boundary
+ * handling, observables and running averages every step.  Enqueued on the
+ * handle's stream as CUDA graphs; returns once enqueued.  Errors of the
+ * device work surface at the next lj_sync / lj_get_* call. */
+lj_status lj_step(lj_system* sys, double dt, int32_t nsteps);
+
+/* Waits for queued work and reports device-side failures (timeouts, NaN). */
+lj_status lj_sync(lj_system* sys);
+
+/* Observables after the last step / force evaluation (synchronises). */
+lj_status lj_get_observables(lj_system* sys, lj_observables* out);
+
+/* Per-step observable records.  lj_set_recording(sys, cap) keeps the last
+ * cap steps (0 disables); lj_get_records copies up to max records, oldest
+ * first, and returns their count in *count. */
+lj_status lj_set_recording(lj_system* sys, int32_t cap);
+lj_status lj_get_records(lj_system* sys, lj_observables* out, int32_t max, int32_t* count);
+
+/* MDSystem::resetAveraging (MDSystem.cpp:701-705). */
+lj_status lj_reset_averaging(lj_system* sys);
+
+/* Setters of MDSystem.h:160-163 (setCanonical, setBoundaryCondition) and the
+ * time step counter's clock (MDSystem::t). */
+lj_status lj_set_canonical(lj_system* sys, int32_t canonical);
+lj_status lj_set_boundary(lj_system* sys, int32_t bc);
+lj_status lj_set_temperature(lj_system* sys, double T0);
+lj_status lj_set_time(lj_system* sys, double t);
+
+/* MDSystem::RenormalizeVelocities (MDSystem.cpp:375-389): scale velocities by
+ * sqrt(T0/Tkin); recalc = 1 measures Tkin from the velocities, 0 uses the
+ * current observable T.  MDSystem::RenormalizeVelocitiesToEnergy
+ * (MDSystem.cpp:391-404): scale so that K = u*N - V. */
+lj_status lj_renormalize_velocities(lj_system* sys, int32_t recalc);
+lj_status lj_renormalize_velocities_to_energy(lj_system* sys, double ust);
+
+/* Pair histogram at the current positions (ordered pairs, as the reference's
+ * NdNdr2 filled inside CalculateForces, MDSystem.cu:39-42 / MDSystem.cpp:281-285).
+ * mode LJ_RDF_R2_*: bins of width `width` in r^2 (the reference's rdf_dr2);
+ * LJ_RDF_R_LINEAR: bins of width `width` in r, r < nbins*width.
+ * nbins <= 4096.  counts: nbins uint64. */
+lj_status lj_rdf_counts(lj_system* sys, int32_t mode, int32_t nbins, double width,
+                        uint64_t* counts);
+
+/* The reference's RDF bin width for N (MDSystem.cpp:93-95), as the float it stores. */
+float lj_reference_rdf_dr2(int32_t n);
+
+/* Speed histogram of initvelo/updatevelo (MDSystem.cpp:651-694): counts of
+ * floor(|v|/step) for bins < nbins.  counts: nbins uint64. */
+lj_status lj_velocity_counts(lj_system* sys, double step, int32_t nbins, uint64_t* counts);
+
+/* Selects the pair-kernel shape by index (see lj_tune_info) or -1 for the
+ * autotuned choice; lj_autotune times every shape now and keeps the fastest. */
+lj_status lj_autotune(lj_system* sys);
+lj_status lj_set_kernel_shape(lj_system* sys, int32_t shape);
+/* Shape table: count, and for shape k its threads per CTA, i-particles per
+ * thread and j-tile length; *active = shape in use. */
+lj_status lj_tune_info(lj_system* sys, int32_t* nshapes, int32_t* active, int32_t k,
+                       int32_t* threads, int32_t* ipt, int32_t* tile);
+
+/* Device-time profiling.  When enabled, each pair-kernel launch inside
+ * lj_step / lj_compute_forces is bracketed by CUDA events on the handle's
+ * stream; lj_profile_read returns the launch count and summed milliseconds
+ * of the pair kernel and of the whole step graph since the last reset. */
+lj_status lj_profile_enable(lj_system* sys, int32_t on);
+lj_status lj_profile_read(lj_system* sys, int64_t* pair_launches, double* pair_ms,
+                          int64_t* steps, double* step_ms);
+
+/* The CUDA stream the handle enqueues on (cudaStream_t as void*).  A caller
+ * may substitute its own stream; NULL restores the handle's private stream. */
+lj_status lj_get_stream(lj_system* sys, void** stream);
+lj_status lj_set_stream(lj_system* sys, void* stream);
+
+/* Number of kernels the library launched on this handle since creation. */
+int64_t lj_kernel_launch_count(const lj_system* sys);
+
+/* ---- Batched replicas ----------------------------------------------------
+ * One handle for nsys independent boxes (uneven N, rho, T0, boundaries),
+ * advanced together: one persistent pair launch per step covers every box.
+ * No counterpart in the reference, which runs one MDSystem per process with
+ * process-global device state (MDSystem.cu:9-18).  All boxes share
+ * precision, device and ensemble (canonical flag). */
+lj_status lj_batch_create(const lj_config* cfgs, int32_t nsys, lj_system** out);
+/* Observables of every box (nsys entries), synchronising. */
+lj_status lj_batch_observables(lj_system* sys, lj_observables* out);
+/* Number of boxes and the particle offset of each (offsets: nsys + 1 entries). */
+lj_status lj_batch_info(const lj_system* sys, int32_t* nsys, int32_t* offsets);
+
+/* ---- Host-side helpers (no device needed) -------------------------------- */
+
+/* The seeded initial state lj_create samples for cfg (N x 3 each): lattice,
+ * jitter, Maxwell speeds, zero momentum, exact T0 (MDSystem.cpp:147-216,
+ * 375-389). */
+lj_status lj_sample_initial_state(const lj_config* cfg, double* pos, double* vel);
+
+/* The stream-K work split the pair kernel uses for boxes n[0..nsys) with
+ * i-blocks of `block` particles, j-tiles of `tile` and at most `ctas` CTAs.
+ * Writes the CTA count, the number of partial segments, the CTA tile ranges
+ * (ctas+1 entries) and, per i-block, 8 ints: box, first particle, particles,
+ * box offset, j-tiles, first segment, segments, first CTA. */
+lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_t tile, int32_t ctas,
+                           int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin,
+                           int32_t* block_info, int32_t max_blocks);
+
+/* Page-locked host memory for lj_set_state / lj_get_state buffers: copies
+ * from and to it run as direct DMA.  NULL on failure; free with lj_host_free. */
+void* lj_host_alloc(size_t bytes);
+void lj_host_free(void* ptr);
+
+/* Library version string and the device architecture it was built for. */
+const char* lj_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LJ_GB300_H */

@@ -1,0 +1,528 @@
+// lj_integrate.cu -- FP64 integrator, boundary, observable and histogram kernels.
+//
+// Replaces the host loops of MDSystem::Integrate (src/library/MDSystem.cpp:438-510),
+// ApplyBoundaryConditions (:406-436), CalculateParameters (:325-359),
+// KineticTemperature (:361-373) and initvelo/updatevelo (:651-694).
+//
+// Layout: positions, velocities, forces are FP64, component-major
+// (x[0..npad) | y | z) so every access of a warp is one coalesced 256-byte
+// segment.  Work is split in the same i-blocks as the pair kernel (one CTA per
+// block).  Every global sum is reduced in a fixed order (block partials, then
+// blocks in index order), so results do not depend on scheduling.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lj_device.cuh"
+#include "lj_kernels.h"
+
+namespace ljgb {
+
+namespace {
+
+constexpr int kObsThreads = 256;
+
+__device__ __forceinline__ void store_shadow(const StateArgs& s, const DevScalars& sc, int p, double x,
+                                             double y, double z) {
+  int4 q;
+  q.x = fixed_coord(x, sc.origin[0], sc.invP);
+  q.y = fixed_coord(y, sc.origin[1], sc.invP);
+  q.z = fixed_coord(z, sc.origin[2], sc.invP);
+  q.w = 0;
+  s.q[p] = q;
+  s.xd[p] = make_double4_32a(x, y, z, 0.0);
+}
+
+// ApplyBoundaryConditions for one particle (MDSystem.cpp:406-436).
+__device__ __forceinline__ void apply_bc(int bc, double L, double (&x)[3], double (&v)[3]) {
+  if (bc == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (x[c] < 0.) x[c] += L;
+      if (x[c] > L) x[c] -= L;
+    }
+  } else if (bc == 1) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (x[c] < 0. && v[c] < 0) v[c] = -v[c];
+      if (x[c] > L && v[c] > 0) v[c] = -v[c];
+    }
+  }
+}
+
+// Block-wide min/max of the positions (for the fixed-point frame of walls /
+// open boxes); result in blk_part[B][0..5].
+__device__ __forceinline__ void block_bbox(const StateArgs& s, int B, bool valid, const double (&x)[3],
+                                           double* sh) {
+  double lo[3], hi[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = valid ? x[c] : 1e300;
+    hi[c] = valid ? x[c] : -1e300;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fmin(lo[c], __shfl_down_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmax(hi[c], __shfl_down_sync(0xffffffffu, hi[c], o));
+    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      sh[c * 32 + warp] = lo[c];
+      sh[(3 + c) * 32 + warp] = hi[c];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < 3; ++c) {
+      double a = 1e300, b = -1e300;
+      for (int w = 0; w < nw; ++w) {
+        a = fmin(a, sh[c * 32 + w]);
+        b = fmax(b, sh[(3 + c) * 32 + w]);
+      }
+      s.blk_part[(size_t)B * 8 + c] = a;
+      s.blk_part[(size_t)B * 8 + 3 + c] = b;
+    }
+  }
+}
+
+// Sum of blk_part[b][slot] over the blocks of one box, fixed order, valid in
+// thread 0 (every CTA that calls this obtains the same bits).
+__device__ __forceinline__ double box_sum(const StateArgs& s, int b0, int b1, int slot, double* sh) {
+  double acc[1] = {0.0};
+  for (int b = b0 + (int)threadIdx.x; b < b1; b += blockDim.x) acc[0] += s.blk_part[(size_t)b * 8 + slot];
+  block_sum<1>(acc, sh);
+  return acc[0];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// First half of the Verlet step (MDSystem.cpp:443-454 EVN, :469-480 TVN):
+//   x += dt v + dt^2 F/2;  EVN: v += dt F/2;  TVN: tF = F/2.
+// Writes the position shadow for periodic boxes; for walls / open boxes it
+// writes the block bounding box instead (the frame follows in k_frame).
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void k_drift(StateArgs s) {
+  __shared__ double sh[6 * 32];
+  const int B = blockIdx.x;
+  const BlockInfo bi = s.blocks[B];
+  const bool valid = (int)threadIdx.x < bi.n_i;
+  const int p = bi.p0 + bi.i0 + threadIdx.x;
+  const BoxArgs box = s.boxes[bi.sys];
+  const double dt = box.dt;
+  double x[3] = {0., 0., 0.};
+  if (valid) {
+    double v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      const double f = s.f[k];
+      x[c] = s.x[k];
+      v[c] = s.v[k];
+      x[c] += dt * v[c] + dt * dt * f / 2.;
+      s.x[k] = x[c];
+      if (MODE == MODE_EVN) s.v[k] = v[c] + dt * f / 2.;
+      if (MODE == MODE_TVN) s.tf[k] = 0.5 * f;
+    }
+    if (box.bc == 0) store_shadow(s, s.sc[bi.sys], p, x[0], x[1], x[2]);
+  }
+  if (box.bc != 0) block_bbox(s, B, valid, x, sh);
+}
+
+// Bounding box of the current positions (initial / injected state).
+__global__ void k_bbox(StateArgs s) {
+  __shared__ double sh[6 * 32];
+  const int B = blockIdx.x;
+  const BlockInfo bi = s.blocks[B];
+  const bool valid = (int)threadIdx.x < bi.n_i;
+  const int p = bi.p0 + bi.i0 + threadIdx.x;
+  double x[3] = {0., 0., 0.};
+  if (valid)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = s.x[(size_t)c * s.npad + p];
+  block_bbox(s, B, valid, x, sh);
+}
+
+// Fixed-point frame per box.  Periodic: origin 0, period L.  Walls / open:
+// origin at the bounding-box minimum, period 2.002 x the largest extent (so
+// no pair separation wraps).  Also the FP32 scale constants of the pair kernel.
+__global__ void k_frame(StateArgs s, int only_nonperiodic) {
+  __shared__ double sh[32];
+  const int sys = blockIdx.x;
+  const BoxArgs box = s.boxes[sys];
+  if (only_nonperiodic && box.bc == 0) return;
+  const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
+  double origin[3] = {0., 0., 0.};
+  double P = box.L;
+  if (box.bc != 0) {
+    double lo[3], hi[3];
+    for (int c = 0; c < 3; ++c) {
+      // min/max over blocks (order-independent)
+      double a = 1e300, b = -1e300;
+      for (int k = b0 + (int)threadIdx.x; k < b1; k += blockDim.x) {
+        a = fmin(a, s.blk_part[(size_t)k * 8 + c]);
+        b = fmax(b, s.blk_part[(size_t)k * 8 + 3 + c]);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        a = fmin(a, __shfl_down_sync(0xffffffffu, a, o));
+        b = fmax(b, __shfl_down_sync(0xffffffffu, b, o));
+      }
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      __syncthreads();
+      if (lane == 0) {
+        sh[warp] = a;
+        sh[16 + warp] = b;
+      }
+      __syncthreads();
+      a = 1e300;
+      b = -1e300;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        a = fmin(a, sh[w]);
+        b = fmax(b, sh[16 + w]);
+      }
+      lo[c] = a;
+      hi[c] = b;
+    }
+    double ext = 0.0;
+    for (int c = 0; c < 3; ++c) ext = fmax(ext, hi[c] - lo[c]);
+    P = 2.002 * ext + 1e-3 * box.sigma;
+    for (int c = 0; c < 3; ++c) origin[c] = lo[c];
+  }
+  if (threadIdx.x == 0) {
+    DevScalars& sc = s.sc[sys];
+    for (int c = 0; c < 3; ++c) sc.origin[c] = origin[c];
+    sc.P = P;
+    sc.invP = 1.0 / P;
+    const double ks = P / (4294967296.0 * box.sigma);
+    sc.k2 = (float)(ks * ks);
+    sc.k2inv = (float)(1.0 / (ks * ks));
+    sc.fscale = 4.0 * box.eps * ks / box.sigma;
+  }
+}
+
+// Writes the fixed-point and FP64 shadows from the FP64 positions.
+__global__ void k_quantize(StateArgs s, int only_nonperiodic) {
+  const int B = blockIdx.x;
+  const BlockInfo bi = s.blocks[B];
+  if (only_nonperiodic && s.boxes[bi.sys].bc == 0) return;
+  if ((int)threadIdx.x >= bi.n_i) return;
+  const int p = bi.p0 + bi.i0 + threadIdx.x;
+  store_shadow(s, s.sc[bi.sys], p, s.x[p], s.x[(size_t)s.npad + p], s.x[2 * (size_t)s.npad + p]);
+}
+
+// ---------------------------------------------------------------------------
+// Sum of the pair-kernel segments into FP64 forces and per-particle sums,
+// then (EVN) the second half-kick + boundaries, or (TVN) the averaged force
+// and the half-kicked velocity whose kinetic temperature sets chi.
+// Block partials: [0] K, [1] V, [2] W, [3] sum tv^2.
+// ---------------------------------------------------------------------------
+template <int MODE, int PREC>
+__global__ void k_reduce(StateArgs s) {
+  __shared__ double sh[4 * 32];
+  const int B = blockIdx.x;
+  const BlockInfo bi = s.blocks[B];
+  const int tid = threadIdx.x;
+  const bool valid = tid < bi.n_i;
+  const int p = bi.p0 + bi.i0 + tid;
+  const BoxArgs box = s.boxes[bi.sys];
+  double part[4] = {0., 0., 0., 0.};
+  if (valid) {
+    double S[5] = {0., 0., 0., 0., 0.};
+    for (int k = 0; k < bi.seg_count; ++k) {
+      const size_t base = (size_t)(bi.seg_first + k) * 5 * s.bi_threads + tid;
+      if (PREC == 0) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) S[c] += (double)s.partial[base + (size_t)c * s.bi_threads];
+      } else {
+        const double* pd = reinterpret_cast<const double*>(s.partial);
+#pragma unroll
+        for (int c = 0; c < 5; ++c) S[c] += pd[base + (size_t)c * s.bi_threads];
+      }
+    }
+    const double fs = (PREC == 0) ? s.sc[bi.sys].fscale : 4.0 * box.eps / (box.sigma * box.sigma);
+    double F[3] = {fs * S[0], fs * S[1], fs * S[2]};
+    const double e = 4.0 * box.eps * (S[3] - S[4]);
+    const double w = 4.0 * box.eps * (12.0 * S[3] - 6.0 * S[4]);
+    s.e[p] = e;
+    s.w[p] = w;
+    part[1] = 0.5 * e;
+    part[2] = w;
+    double x[3], v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      s.f[k] = F[c];
+      v[c] = s.v[k];
+    }
+    if (MODE == MODE_FORCES_ONLY) {
+      part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    } else if (MODE == MODE_EVN) {
+      const double dt = box.dt;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        v[c] += dt * F[c] / 2.;
+        x[c] = s.x[(size_t)c * s.npad + p];
+      }
+      apply_bc(box.bc, box.L, x, v);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        s.v[(size_t)c * s.npad + p] = v[c];
+        if (box.bc == 0) s.x[(size_t)c * s.npad + p] = x[c];
+      }
+      part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    } else {  // TVN
+      const double dt = box.dt;
+      double tv2 = 0.0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t k = (size_t)c * s.npad + p;
+        const double tf = s.tf[k] + 0.5 * F[c];
+        s.tf[k] = tf;
+        const double tv = v[c] + dt * tf / 2.;
+        tv2 += tv * tv;
+      }
+      part[3] = tv2;
+    }
+  }
+  block_sum<4>(part, sh);
+  if (tid == 0) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
+  }
+}
+
+// TVN velocity update (MDSystem.cpp:498-506): chi = sqrt(T0 / Tkin(tv)),
+// v = (2 chi - 1) v + chi dt tF, then boundaries; block partial [0] = K.
+__global__ void k_tvn_finish(StateArgs s) {
+  __shared__ double sh[32];
+  __shared__ double chi_sh;
+  const int B = blockIdx.x;
+  const BlockInfo bi = s.blocks[B];
+  const int tid = threadIdx.x;
+  const BoxArgs box = s.boxes[bi.sys];
+  const int b0 = s.sys_block_first[bi.sys], b1 = s.sys_block_first[bi.sys + 1];
+  const double tv2 = box_sum(s, b0, b1, 3, sh);
+  if (tid == 0) {
+    const double Tkin = tv2 * (1. / 3. / box.N);
+    const double chi = sqrt(box.T0 / Tkin);
+    chi_sh = chi;
+    if (B == b0) {
+      s.sc[bi.sys].Tkin = Tkin;
+      s.sc[bi.sys].chi = chi;
+    }
+  }
+  __syncthreads();
+  const double chi = chi_sh;
+  double part[1] = {0.0};
+  if (tid < bi.n_i) {
+    const int p = bi.p0 + bi.i0 + tid;
+    double x[3], v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      v[c] = (2. * chi - 1.) * s.v[k] + chi * box.dt * s.tf[k];
+      x[c] = s.x[k];
+    }
+    apply_bc(box.bc, box.L, x, v);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      s.v[k] = v[c];
+      if (box.bc == 0) s.x[k] = x[c];
+    }
+    part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  }
+  __syncthreads();
+  block_sum<1>(part, sh);
+  if (tid == 0) s.blk_part[(size_t)B * 8 + 0] = part[0];
+}
+
+// CalculateParameters (MDSystem.cpp:325-359) per box, plus t += dt for steps
+// (MDSystem.cpp:582) and the optional per-step record.
+template <int MODE>
+__global__ void k_observables(StateArgs s) {
+  __shared__ double sh[32];
+  const int sys = blockIdx.x;
+  const BoxArgs box = s.boxes[sys];
+  const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
+  const double K = box_sum(s, b0, b1, 0, sh);
+  const double V = box_sum(s, b0, b1, 1, sh);
+  const double W = box_sum(s, b0, b1, 2, sh);
+  if (threadIdx.x != 0) return;
+  DevScalars& sc = s.sc[sys];
+  const double N = (double)box.N;
+  const double T = 2. * K / 3. / N;
+  const double P = (W / 6. + N * T) / (N / box.rho);
+  const double U = K + V;
+  sc.K = K;
+  sc.V = V;
+  sc.W = W;
+  sc.T = T;
+  sc.P_press = P;
+  sc.U = U;
+  if (MODE != MODE_TVN) sc.Tkin = 0.0;
+  if (MODE != MODE_FORCES_ONLY) {
+    sc.t += box.dt;
+    sc.step += 1;
+  }
+  sc.av_iters += 1;
+  sc.av_U += U;
+  sc.av_p += P;
+  sc.av_T += T;
+  if (!isfinite(K) || !isfinite(V) || !isfinite(W)) atomicOr(s.status, LJ_DEVFLAG_NONFINITE);
+  if (sc.rec_cap > 0 && MODE != MODE_FORCES_ONLY) {
+    DevRecord& r = s.records[(size_t)sys * s.rec_stride + (size_t)(sc.rec_count % sc.rec_cap)];
+    r.t = sc.t;
+    r.K = K;
+    r.V = V;
+    r.T = T;
+    r.P = P;
+    r.U = U;
+    r.W = W;
+    r.Pshear = sc.Pshear;
+    r.Tkin = sc.Tkin;
+    r.av_U = sc.av_U;
+    r.av_T = sc.av_T;
+    r.av_p = sc.av_p;
+    r.av_iters = sc.av_iters;
+    r.step = sc.step;
+    sc.rec_count += 1;
+  }
+}
+
+// |v| histogram (MDSystem.cpp:658-662): b = floor(sqrt(v.v)/step), b < nb.
+// Products and sums rounded separately so the bins are reproducible on a CPU.
+__global__ void k_velocity_hist(StateArgs s, double step, int nb, unsigned long long* counts) {
+  __shared__ unsigned hist[kMaxHistBins];
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) hist[b] = 0u;
+  __syncthreads();
+  const BlockInfo bi = s.blocks[blockIdx.x];
+  if ((int)threadIdx.x < bi.n_i) {
+    const int p = bi.p0 + bi.i0 + threadIdx.x;
+    const double vx = s.v[p], vy = s.v[(size_t)s.npad + p], vz = s.v[2 * (size_t)s.npad + p];
+    double q = __dmul_rn(vx, vx);
+    q = __dadd_rn(q, __dmul_rn(vy, vy));
+    q = __dadd_rn(q, __dmul_rn(vz, vz));
+    const double b = floor(__ddiv_rn(__dsqrt_rn(q), step));
+    if (b < (double)nb) atomicAdd(&hist[(int)b], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    if (hist[b]) atomicAdd(counts + b, (unsigned long long)hist[b]);
+}
+
+// sysmode 0: v *= factor.  sysmode 1: block partial [0] = sum v^2 / 2 (for
+// RenormalizeVelocities with Tkin recomputed).
+__global__ void k_velocities(StateArgs s, int sysmode, double factor) {
+  __shared__ double sh[32];
+  const int B = blockIdx.x;
+  const BlockInfo bi = s.blocks[B];
+  double part[1] = {0.0};
+  if ((int)threadIdx.x < bi.n_i) {
+    const int p = bi.p0 + bi.i0 + threadIdx.x;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      const double v = s.v[k];
+      if (sysmode == 0) s.v[k] = v * factor;
+      part[0] += v * v;
+    }
+    part[0] *= 0.5;
+  }
+  if (sysmode == 1) {
+    block_sum<1>(part, sh);
+    if (threadIdx.x == 0) s.blk_part[(size_t)B * 8 + 0] = part[0];
+  }
+}
+
+// Interleaved (x,y,z per particle) <-> component-major, all boxes at once.
+__global__ void k_unpack(const double* __restrict__ in, double* __restrict__ out, int n, int npad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
+}
+
+__global__ void k_pack(const double* __restrict__ in, double* __restrict__ out, int n, int npad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[3 * (size_t)i + c] = in[(size_t)c * npad + i];
+}
+
+// ---------------------------------------------------------------------------
+// Launchers.
+// ---------------------------------------------------------------------------
+cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st) {
+  k_unpack<<<(n + 255) / 256, 256, 0, st>>>(in, out, n, npad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st) {
+  k_pack<<<(n + 255) / 256, 256, 0, st>>>(in, out, n, npad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_drift_mode(const StateArgs& s, int nblocks, int bi, int mode, cudaStream_t st) {
+  if (mode == MODE_EVN) k_drift<MODE_EVN><<<nblocks, bi, 0, st>>>(s);
+  else k_drift<MODE_TVN><<<nblocks, bi, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bbox(const StateArgs& s, int nblocks, int bi, cudaStream_t st) {
+  k_bbox<<<nblocks, bi, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frame(const StateArgs& s, int nsys, bool only_nonperiodic, cudaStream_t st) {
+  k_frame<<<nsys, kObsThreads, 0, st>>>(s, only_nonperiodic ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_quantize(const StateArgs& s, int nblocks, int bi, bool only_nonperiodic, cudaStream_t st) {
+  k_quantize<<<nblocks, bi, 0, st>>>(s, only_nonperiodic ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const StateArgs& s, int nblocks, int bi, int mode, cudaStream_t st) {
+  if (s.prec == 0) {
+    if (mode == MODE_FORCES_ONLY) k_reduce<MODE_FORCES_ONLY, 0><<<nblocks, bi, 0, st>>>(s);
+    else if (mode == MODE_EVN) k_reduce<MODE_EVN, 0><<<nblocks, bi, 0, st>>>(s);
+    else k_reduce<MODE_TVN, 0><<<nblocks, bi, 0, st>>>(s);
+  } else {
+    if (mode == MODE_FORCES_ONLY) k_reduce<MODE_FORCES_ONLY, 1><<<nblocks, bi, 0, st>>>(s);
+    else if (mode == MODE_EVN) k_reduce<MODE_EVN, 1><<<nblocks, bi, 0, st>>>(s);
+    else k_reduce<MODE_TVN, 1><<<nblocks, bi, 0, st>>>(s);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tvn_finish(const StateArgs& s, int nblocks, int bi, cudaStream_t st) {
+  k_tvn_finish<<<nblocks, bi, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_observables(const StateArgs& s, int nsys, int mode, cudaStream_t st) {
+  if (mode == MODE_FORCES_ONLY) k_observables<MODE_FORCES_ONLY><<<nsys, kObsThreads, 0, st>>>(s);
+  else if (mode == MODE_EVN) k_observables<MODE_EVN><<<nsys, kObsThreads, 0, st>>>(s);
+  else k_observables<MODE_TVN><<<nsys, kObsThreads, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_velocity_hist(const StateArgs& s, int nblocks, int bi, double step, int nb,
+                                 unsigned long long* counts, cudaStream_t st) {
+  k_velocity_hist<<<nblocks, bi, 0, st>>>(s, step, nb, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double factor,
+                                    cudaStream_t st) {
+  k_velocities<<<nblocks, bi, 0, st>>>(s, sysmode, factor);
+  return cudaGetLastError();
+}
+
+}  // namespace ljgb

@@ -1,0 +1,69 @@
+// lj_internal.h -- host/device shared structures of the LJ GB300 library.
+#pragma once
+
+#include <cstdint>
+
+namespace ljgb {
+
+// Device-side status flags (DevScalars::status).
+enum : int {
+  LJ_DEVFLAG_TIMEOUT = 1,    // a bounded mbarrier wait gave up
+  LJ_DEVFLAG_NONFINITE = 2,  // NaN/Inf observable
+};
+
+// Per-system frame of the fixed-point shadow and the scalar state that the
+// kernels update on the device.  One per simulated box; kept in device memory
+// so captured step graphs read current values.
+struct DevScalars {
+  // fixed-point frame: q = frac((x - origin)/P) * 2^32
+  double origin[3];
+  double P, invP;
+  float k2inv;    // 1 / (P / (2^32 sigma))^2  : sigma^2 / r^2 = k2inv / r2_fixed
+  float k2;       // (P / (2^32 sigma))^2       : r^2 / sigma^2 = k2 * r2_fixed
+  double fscale;  // F = fscale * sum s * d_fixed   (4 eps * k_sigma / sigma)
+  // clock and running averages (MDSystem.h:80, 98-99)
+  double t;
+  long long step;
+  double av_U, av_T, av_p;
+  long long av_iters;
+  // last observables (MDSystem.h:63-66)
+  double K, V, T, P_press, U, W, Pshear, Tkin;
+  // TVN scale of the last step
+  double chi;
+  int status;
+  int rec_cap;
+  long long rec_count;
+};
+
+// Observable record layout written by the device (matches lj_observables).
+struct DevRecord {
+  double t, K, V, T, P, U, W, Pshear, Tkin, av_U, av_T, av_p;
+  long long av_iters, step;
+};
+
+// One i-block of the stream-K schedule: BI consecutive particles of one box.
+struct BlockInfo {
+  int sys;        // box index
+  int i0;         // first box-local particle of the block
+  int n_i;        // valid particles in the block (<= BI)
+  int p0;         // global offset of the box's particle 0
+  int n_sys;      // particles in the box
+  int njt;        // j-tiles of the box
+  int seg_first;  // first partial segment of this block
+  int seg_count;  // segments of this block
+  int g_first;    // first CTA that processes this block
+  int pad;
+};
+
+// Per-box constants passed by value (captured into graphs).
+struct BoxArgs {
+  int N;
+  int bc;
+  int canonical;
+  int pad;
+  double L, invL;
+  double eps, sigma;
+  double dt, T0, rho;
+};
+
+}  // namespace ljgb

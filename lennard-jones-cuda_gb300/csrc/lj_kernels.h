@@ -1,0 +1,98 @@
+// lj_kernels.h -- launch interface of the LJ kernels (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lj_internal.h"
+
+namespace ljgb {
+
+constexpr int kMaxHistBins = 4096;
+
+// Pair-histogram request.  mode 0: r^2 bins, clamp overflow to the last bin
+// (MDSystem.cu:39); 1: r^2 bins, drop overflow (MDSystem.cpp:282-284);
+// 2: linear r bins up to rmax (pairs with r >= rmax dropped).
+struct HistArgs {
+  int mode;
+  int nb;
+  float inv_w;   // 1/dr2 (modes 0,1) or 1/dr (mode 2)
+  float rmax2;   // mode 2: rmax^2 in sigma^2
+  unsigned long long* counts;  // nb counters (global, accumulated with atomics)
+};
+
+// Arguments of the persistent pair kernels (by value).
+struct PairArgs {
+  const int4* q;              // MIXED: fixed-point shadow (x, y, z, pad), all boxes
+  const double4_32a* xd;          // FP64: position shadow (x, y, z, 0)
+  const BlockInfo* blocks;    // i-blocks of the schedule
+  const int* cta_tile_begin;  // G+1 tile ranges
+  const int* cta_block;       // first i-block of each CTA
+  const int* cta_jt;          // first j-tile (within that block) of each CTA
+  const DevScalars* sc;       // per box frame / scalars
+  const BoxArgs* boxes;       // per box constants
+  float* partial;             // nseg x 5 x threads  (float, or double for FP64)
+  int* status;                // device status word (timeouts)
+  HistArgs hist;
+};
+
+struct PairShape {
+  int threads;  // CTA size = i-block length (one i per thread)
+  int tile;     // j records per staged tile
+  int stages;   // depth of the bulk-copy ring
+};
+
+extern const PairShape kShapes[];
+extern const int kNumShapes;
+int fp64_block_threads();
+int fp64_tile();
+
+cudaError_t pair_occupancy(int prec, int shape, int* blocks_per_sm);
+cudaError_t launch_pairs(int prec, int shape, bool forces, bool hist, const PairArgs& a, int grid,
+                         cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Integrator / reduction kernels (lj_integrate.cu).  All operate on the
+// i-block decomposition: grid = number of blocks, blockDim = BI.
+// ---------------------------------------------------------------------------
+struct StateArgs {
+  double* x;        // 3 x Npad, component-major (x | y | z)
+  double* v;        // 3 x Npad
+  double* f;        // 3 x Npad, forces
+  double* tf;       // 3 x Npad, TVN averaged force (F_old + F_new)/2
+  double* e;        // Npad per-particle pair energy sum  4eps sum [(s/r)^12-(s/r)^6]
+  double* w;        // Npad per-particle virial sum  sum r.f
+  int4* q;          // fixed-point shadow
+  double4_32a* xd;      // FP64 position shadow
+  int npad;         // stride between components
+  const BlockInfo* blocks;
+  const BoxArgs* boxes;
+  DevScalars* sc;
+  const int* sys_block_first;  // nsys + 1
+  double* blk_part;            // nblocks x 8 partial sums
+  const float* partial;        // pair-kernel partials
+  int prec;                    // LJ_PREC_*
+  int bi_threads;              // threads of the pair kernel's i-block (partial stride)
+  DevRecord* records;          // per box ring (rec_cap entries each)
+  int rec_stride;              // ring capacity per box
+  int* status;
+};
+
+enum StepMode { MODE_FORCES_ONLY = 0, MODE_EVN = 1, MODE_TVN = 2 };
+
+cudaError_t launch_drift_mode(const StateArgs& s, int nblocks, int bi, int mode, cudaStream_t st);
+cudaError_t launch_bbox(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
+cudaError_t launch_frame(const StateArgs& s, int nsys, bool only_nonperiodic, cudaStream_t st);
+cudaError_t launch_quantize(const StateArgs& s, int nblocks, int bi, bool only_nonperiodic, cudaStream_t st);
+cudaError_t launch_reduce(const StateArgs& s, int nblocks, int bi, int mode, cudaStream_t st);
+cudaError_t launch_tvn_finish(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
+cudaError_t launch_observables(const StateArgs& s, int nsys, int mode, cudaStream_t st);
+cudaError_t launch_velocity_hist(const StateArgs& s, int nblocks, int bi, double step, int nb,
+                                 unsigned long long* counts, cudaStream_t st);
+cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
+cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st);
+cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,
+                                    cudaStream_t st);
+
+}  // namespace ljgb

@@ -1,0 +1,416 @@
+// lj_pairs.cu -- all-pairs Lennard-Jones force / energy / virial / RDF kernels.
+//
+// Replaces calculateForces + RDFmerger of the reference
+// (src/library/MDSystem.cu:21-153) and the O(N^2) CPU loop of
+// MDSystem::CalculateForces (src/library/MDSystem.cpp:253-310).  Same pair set
+// (ordered pairs j != i, minimum image for periodic boxes, no cutoff), same
+// physics (MDSystem.cu:44-53), redesigned for sm_103a:
+//
+//  * persistent stream-K grid: every CTA receives an equal share of the
+//    (i-block, j-tile) sequence of all boxes, so the single wave fills all
+//    SMs regardless of N (the reference launches ceil(N/256) CTAs);
+//  * j-tiles of 16-byte records staged in shared memory by cp.async.bulk
+//    (TMA bulk copies) into a STAGES-deep mbarrier ring, read back as
+//    broadcast 128-bit shared loads;
+//  * MIXED precision: positions as 32-bit fixed-point fractions of the box
+//    whose wrapping integer difference is the minimum image (no rounding
+//    instructions per pair), FP32 pair math, per-tile FP32 sums folded into
+//    TwoSum-compensated accumulators;
+//  * no per-pair global atomics: partial sums of each (CTA, i-block) segment
+//    go to a partial buffer reduced deterministically in FP64 by the
+//    integrator kernels; pair histograms (RDF) go to a shared-memory
+//    histogram flushed once per CTA.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lj_device.cuh"
+#include "lj_kernels.h"
+
+namespace ljgb {
+
+namespace {
+
+// One pair in the MIXED path.  d = qi - qj wraps to the minimum image.
+// s = (s/r)^8 [12 (s/r)^6 - 6] (sigma units), a += (s/r)^12, b += (s/r)^6.
+template <bool MASKED>
+__device__ __forceinline__ void pair_mixed(const int4 qi, const int4 qj, float k2inv, bool excl,
+                                           float& fx, float& fy, float& fz, float& pa,
+                                           float& pb) {
+  const float dx = __int2float_rn((int)((unsigned)qi.x - (unsigned)qj.x));
+  const float dy = __int2float_rn((int)((unsigned)qi.y - (unsigned)qj.y));
+  const float dz = __int2float_rn((int)((unsigned)qi.z - (unsigned)qj.z));
+  const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+  float ri = __fdividef(k2inv, r2);
+  if (MASKED) ri = excl ? 0.0f : ri;
+  const float r6 = ri * ri * ri;
+  const float t = __fmaf_rn(12.0f, r6, -6.0f);
+  const float s = r6 * ri * t;
+  fx = __fmaf_rn(s, dx, fx);
+  fy = __fmaf_rn(s, dy, fy);
+  fz = __fmaf_rn(s, dz, fz);
+  pa = __fmaf_rn(r6, r6, pa);
+  pb += r6;
+}
+
+// Histogram bin of a pair from its fixed-point separation; the arithmetic is
+// exactly what the oracle's emu_rdf_* reproduces on the CPU.
+__device__ __forceinline__ int pair_bin(const int4 qi, const int4 qj, float k2, const HistArgs& h) {
+  const float dx = __int2float_rn((int)((unsigned)qj.x - (unsigned)qi.x));
+  const float dy = __int2float_rn((int)((unsigned)qj.y - (unsigned)qi.y));
+  const float dz = __int2float_rn((int)((unsigned)qj.z - (unsigned)qi.z));
+  const float r2 = __fmul_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), k2);
+  if (h.mode == 2) {  // linear r bins, r < rmax
+    if (!(r2 < h.rmax2)) return -1;
+    int b = (int)floorf(__fmul_rn(__fsqrt_rn(r2), h.inv_w));
+    return b > h.nb - 1 ? h.nb - 1 : b;
+  }
+  const float fb = floorf(__fmul_rn(r2, h.inv_w));
+  if (h.mode == 0) return fb < (float)(h.nb - 1) ? (int)fb : h.nb - 1;  // clamp (MDSystem.cu:39)
+  return fb < (float)h.nb ? (int)fb : -1;                               // drop (MDSystem.cpp:283)
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// MIXED-precision persistent pair kernel.
+// THREADS threads, one i-particle each; TILE j-records per stage.
+// ---------------------------------------------------------------------------
+template <int THREADS, int TILE, int STAGES, bool FORCES, bool HIST>
+__global__ void __launch_bounds__(THREADS) k_pairs_mixed(PairArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  int4* sq = reinterpret_cast<int4*>(smem_raw);
+  unsigned* shist = reinterpret_cast<unsigned*>(smem_raw + sizeof(int4) * STAGES * TILE);
+  __shared__ uint64_t bars[STAGES];
+
+  const int g = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int t0 = a.cta_tile_begin[g], t1 = a.cta_tile_begin[g + 1];
+  const int ntiles = t1 - t0;
+  if (ntiles <= 0) return;
+
+  if (HIST) {
+    for (int b = tid; b < a.hist.nb; b += THREADS) shist[b] = 0u;
+  }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // Producer cursor (thread 0): next tile to copy.
+  int pB = a.cta_block[g], pjt = a.cta_jt[g], issued = 0;
+  if (tid == 0) {
+    const int pre = ntiles < STAGES ? ntiles : STAGES;
+    for (; issued < pre; ++issued) {
+      const BlockInfo bi = a.blocks[pB];
+      const int j0 = pjt * TILE;
+      const int cnt = min(TILE, bi.n_sys - j0);
+      const int s = issued % STAGES;
+      mbar_arrive_expect_tx(&bars[s], (uint32_t)cnt * 16u);
+      bulk_g2s(sq + s * TILE, a.q + bi.p0 + j0, (uint32_t)cnt * 16u, &bars[s]);
+      if (++pjt == bi.njt) { ++pB; pjt = 0; }
+    }
+  }
+
+  int B = a.cta_block[g], jt = a.cta_jt[g];
+  BlockInfo bi = a.blocks[B];
+  int i_local = bi.i0 + tid;
+  bool valid_i = tid < bi.n_i;
+  int4 qi = a.q[bi.p0 + (valid_i ? i_local : bi.i0)];
+  float k2inv = a.sc[bi.sys].k2inv;
+  float k2 = a.sc[bi.sys].k2;
+  FloatAcc acc[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
+
+  int k = 0;
+  bool failed = false;
+  for (; k < ntiles; ++k) {
+    const int s = k % STAGES;
+    const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((k / STAGES) & 1));
+    const int j0 = jt * TILE;
+    const int cnt = min(TILE, bi.n_sys - j0);
+    if (ok) {
+      const int4* st = sq + s * TILE;
+      const bool masked = (cnt < TILE) || (j0 < bi.i0 + bi.n_i && j0 + cnt > bi.i0);
+      if (FORCES) {
+        float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
+        if (!masked) {
+#pragma unroll 8
+          for (int jj = 0; jj < TILE; ++jj) pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb);
+        } else {
+          for (int jj = 0; jj < cnt; ++jj)
+            pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb);
+        }
+        two_sum_add(acc[0], fx);
+        two_sum_add(acc[1], fy);
+        two_sum_add(acc[2], fz);
+        two_sum_add(acc[3], pa);
+        two_sum_add(acc[4], pb);
+      }
+      if (HIST && valid_i) {
+        for (int jj = 0; jj < cnt; ++jj) {
+          if (j0 + jj == i_local) continue;
+          const int b = pair_bin(qi, st[jj], k2, a.hist);
+          if (b >= 0) atomicAdd(&shist[b], 1u);
+        }
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    // Stage s is free again: refill it with the tile STAGES ahead.
+    if (tid == 0 && issued < ntiles) {
+      const BlockInfo pbi = a.blocks[pB];
+      const int pj0 = pjt * TILE;
+      const int pcnt = min(TILE, pbi.n_sys - pj0);
+      mbar_arrive_expect_tx(&bars[s], (uint32_t)pcnt * 16u);
+      bulk_g2s(sq + s * TILE, a.q + pbi.p0 + pj0, (uint32_t)pcnt * 16u, &bars[s]);
+      if (++pjt == pbi.njt) { ++pB; pjt = 0; }
+      ++issued;
+    }
+    const bool last = (k == ntiles - 1);
+    const bool block_end = (jt + 1 == bi.njt);
+    if (block_end || last) {
+      if (FORCES && valid_i) {
+        const int seg = bi.seg_first + (g - bi.g_first);
+        float* out = a.partial + (size_t)seg * 5 * THREADS;
+#pragma unroll
+        for (int c = 0; c < 5; ++c) out[c * THREADS + tid] = acc[c].hi + acc[c].lo;
+      }
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
+      if (block_end && !last) {
+        ++B;
+        bi = a.blocks[B];
+        i_local = bi.i0 + tid;
+        valid_i = tid < bi.n_i;
+        qi = a.q[bi.p0 + (valid_i ? i_local : bi.i0)];
+        k2inv = a.sc[bi.sys].k2inv;
+        k2 = a.sc[bi.sys].k2;
+        jt = 0;
+      }
+    } else {
+      ++jt;
+    }
+  }
+
+  if (failed) {
+    // Drain the copies still in flight before the CTA's shared memory goes away.
+    if (tid == 0) {
+      for (int kk = k; kk < issued; ++kk) mbar_wait_bounded(&bars[kk % STAGES], (uint32_t)((kk / STAGES) & 1));
+      atomicOr(a.status, LJ_DEVFLAG_TIMEOUT);
+    }
+    return;
+  }
+  if (HIST) {
+    __syncthreads();
+    for (int b = tid; b < a.hist.nb; b += THREADS)
+      if (shist[b]) atomicAdd(a.hist.counts + b, (unsigned long long)shist[b]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// All-FP64 persistent pair kernel (the comparator path): double positions,
+// minimum image by rint, double accumulators.  Same schedule and partials
+// layout (5 doubles per particle per segment).
+// ---------------------------------------------------------------------------
+template <int THREADS, int TILE, int STAGES>
+__global__ void __launch_bounds__(THREADS) k_pairs_fp64(PairArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double4_32a* sx = reinterpret_cast<double4_32a*>(smem_raw);
+  __shared__ uint64_t bars[STAGES];
+
+  const int g = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int t0 = a.cta_tile_begin[g], t1 = a.cta_tile_begin[g + 1];
+  const int ntiles = t1 - t0;
+  if (ntiles <= 0) return;
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int pB = a.cta_block[g], pjt = a.cta_jt[g], issued = 0;
+  if (tid == 0) {
+    const int pre = ntiles < STAGES ? ntiles : STAGES;
+    for (; issued < pre; ++issued) {
+      const BlockInfo bi = a.blocks[pB];
+      const int j0 = pjt * TILE;
+      const int cnt = min(TILE, bi.n_sys - j0);
+      const int s = issued % STAGES;
+      mbar_arrive_expect_tx(&bars[s], (uint32_t)cnt * 32u);
+      bulk_g2s(sx + s * TILE, a.xd + bi.p0 + j0, (uint32_t)cnt * 32u, &bars[s]);
+      if (++pjt == bi.njt) { ++pB; pjt = 0; }
+    }
+  }
+
+  int B = a.cta_block[g], jt = a.cta_jt[g];
+  BlockInfo bi = a.blocks[B];
+  int i_local = bi.i0 + tid;
+  bool valid_i = tid < bi.n_i;
+  double4_32a xi = a.xd[bi.p0 + (valid_i ? i_local : bi.i0)];
+  BoxArgs box = a.boxes[bi.sys];
+  double s2 = box.sigma * box.sigma;
+  bool periodic = box.bc == 0;
+  double ax = 0., ay = 0., az = 0., aa = 0., ab = 0.;
+
+  int k = 0;
+  bool failed = false;
+  for (; k < ntiles; ++k) {
+    const int s = k % STAGES;
+    const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((k / STAGES) & 1));
+    const int j0 = jt * TILE;
+    const int cnt = min(TILE, bi.n_sys - j0);
+    if (ok) {
+      const double4_32a* st = sx + s * TILE;
+      for (int jj = 0; jj < cnt; ++jj) {
+        const double4_32a xj = st[jj];
+        double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        if (periodic) {
+          dx = fma(-box.L, rint(dx * box.invL), dx);
+          dy = fma(-box.L, rint(dy * box.invL), dy);
+          dz = fma(-box.L, rint(dz * box.invL), dz);
+        }
+        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+        double ri = s2 / r2;
+        if (j0 + jj == i_local) ri = 0.0;
+        const double r6 = ri * ri * ri;
+        const double sf = r6 * ri * fma(12.0, r6, -6.0);
+        ax = fma(sf, dx, ax);
+        ay = fma(sf, dy, ay);
+        az = fma(sf, dz, az);
+        aa = fma(r6, r6, aa);
+        ab += r6;
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    if (tid == 0 && issued < ntiles) {
+      const BlockInfo pbi = a.blocks[pB];
+      const int pj0 = pjt * TILE;
+      const int pcnt = min(TILE, pbi.n_sys - pj0);
+      mbar_arrive_expect_tx(&bars[s], (uint32_t)pcnt * 32u);
+      bulk_g2s(sx + s * TILE, a.xd + pbi.p0 + pj0, (uint32_t)pcnt * 32u, &bars[s]);
+      if (++pjt == pbi.njt) { ++pB; pjt = 0; }
+      ++issued;
+    }
+    const bool last = (k == ntiles - 1);
+    const bool block_end = (jt + 1 == bi.njt);
+    if (block_end || last) {
+      if (valid_i) {
+        const int seg = bi.seg_first + (g - bi.g_first);
+        double* out = reinterpret_cast<double*>(a.partial) + (size_t)seg * 5 * THREADS;
+        out[0 * THREADS + tid] = ax;
+        out[1 * THREADS + tid] = ay;
+        out[2 * THREADS + tid] = az;
+        out[3 * THREADS + tid] = aa;
+        out[4 * THREADS + tid] = ab;
+      }
+      ax = ay = az = aa = ab = 0.;
+      if (block_end && !last) {
+        ++B;
+        bi = a.blocks[B];
+        i_local = bi.i0 + tid;
+        valid_i = tid < bi.n_i;
+        xi = a.xd[bi.p0 + (valid_i ? i_local : bi.i0)];
+        box = a.boxes[bi.sys];
+        s2 = box.sigma * box.sigma;
+        periodic = box.bc == 0;
+        jt = 0;
+      }
+    } else {
+      ++jt;
+    }
+  }
+  if (failed && tid == 0) {
+    for (int kk = k; kk < issued; ++kk) mbar_wait_bounded(&bars[kk % STAGES], (uint32_t)((kk / STAGES) & 1));
+    atomicOr(a.status, LJ_DEVFLAG_TIMEOUT);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shape table and launchers.
+// ---------------------------------------------------------------------------
+namespace {
+
+template <int THREADS, int TILE, int STAGES, bool FORCES, bool HIST>
+cudaError_t launch_mixed_t(const PairArgs& a, int grid, cudaStream_t st) {
+  // <= 48 KB: 16 B x STAGES x TILE staging (+ 16 KB histogram), no opt-in needed.
+  const size_t smem = sizeof(int4) * STAGES * TILE + (HIST ? sizeof(unsigned) * kMaxHistBins : 0);
+  k_pairs_mixed<THREADS, TILE, STAGES, FORCES, HIST><<<grid, THREADS, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int THREADS, int TILE, int STAGES>
+cudaError_t occupancy_mixed_t(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      blocks_per_sm, k_pairs_mixed<THREADS, TILE, STAGES, true, false>, THREADS,
+      sizeof(int4) * STAGES * TILE);
+}
+
+template <int THREADS, int TILE, int STAGES>
+cudaError_t launch_fp64_t(const PairArgs& a, int grid, cudaStream_t st) {
+  const size_t smem = sizeof(double4_32a) * STAGES * TILE;
+  k_pairs_fp64<THREADS, TILE, STAGES><<<grid, THREADS, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int THREADS, int TILE, int STAGES>
+cudaError_t occupancy_fp64_t(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_pairs_fp64<THREADS, TILE, STAGES>,
+                                                       THREADS, sizeof(double4_32a) * STAGES * TILE);
+}
+
+}  // namespace
+
+// Kernel shapes the autotuner chooses among (threads = i-block size).
+const PairShape kShapes[] = {
+    {128, 256, 3},
+    {64, 256, 3},
+    {256, 256, 3},
+    {128, 512, 2},
+};
+const int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+
+// FP64 i-block and j-tile match MIXED shape 0 so the histogram kernel can
+// run on an FP64 handle's schedule.
+constexpr int kFp64Threads = 128, kFp64Tile = 256, kFp64Stages = 3;
+
+int fp64_block_threads() { return kFp64Threads; }
+int fp64_tile() { return kFp64Tile; }
+
+cudaError_t pair_occupancy(int prec, int shape, int* blocks_per_sm) {
+  if (prec == 1) return occupancy_fp64_t<kFp64Threads, kFp64Tile, kFp64Stages>(blocks_per_sm);
+  switch (shape) {
+    case 0: return occupancy_mixed_t<128, 256, 3>(blocks_per_sm);
+    case 1: return occupancy_mixed_t<64, 256, 3>(blocks_per_sm);
+    case 2: return occupancy_mixed_t<256, 256, 3>(blocks_per_sm);
+    case 3: return occupancy_mixed_t<128, 512, 2>(blocks_per_sm);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pairs(int prec, int shape, bool forces, bool hist, const PairArgs& a, int grid,
+                         cudaStream_t st) {
+  if (prec == 1) return launch_fp64_t<kFp64Threads, kFp64Tile, kFp64Stages>(a, grid, st);
+#define LJ_DISPATCH(T, TL, S)                                                     \
+  if (forces && !hist) return launch_mixed_t<T, TL, S, true, false>(a, grid, st); \
+  if (forces && hist) return launch_mixed_t<T, TL, S, true, true>(a, grid, st);   \
+  return launch_mixed_t<T, TL, S, false, true>(a, grid, st);
+  switch (shape) {
+    case 0: { LJ_DISPATCH(128, 256, 3) }
+    case 1: { LJ_DISPATCH(64, 256, 3) }
+    case 2: { LJ_DISPATCH(256, 256, 3) }
+    case 3: { LJ_DISPATCH(128, 512, 2) }
+  }
+#undef LJ_DISPATCH
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ljgb

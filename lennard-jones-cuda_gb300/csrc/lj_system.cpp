@@ -1,0 +1,1189 @@
+// lj_system.cpp -- the lj_* C ABI: handle lifetime, device memory, step
+// graphs, observables, histograms, autotuning and profiling.
+//
+// One lj_system owns one or more boxes (a batch shares one persistent pair
+// launch per step).  Host code never loops over particles except to sample the
+// initial state; all per-step work runs in the kernels of lj_pairs.cu and
+// lj_integrate.cu, enqueued on the handle's stream as captured CUDA graphs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "lj_gb300.h"
+#include "lj_init.h"
+#include "lj_kernels.h"
+#include "lj_schedule.h"
+
+using namespace ljgb;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// Tile overhead in j-record units (barrier, compensation, refill) used to
+// weight ragged tiles in the stream-K split.
+constexpr int kTileOverhead = 8;
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * count);
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct GraphEntry {
+  cudaGraphExec_t exec = nullptr;
+  int kernels = 0;
+  bool profiled = false;
+  cudaGraphNode_t ev_nodes[4] = {nullptr, nullptr, nullptr, nullptr};  // step start, pair start, pair end, step end
+};
+
+}  // namespace
+
+struct lj_system {
+  // configuration per box
+  std::vector<lj_config> cfg;
+  std::vector<BoxArgs> boxes;
+  int nsys = 0;
+  int ntotal = 0;  // particles over all boxes
+  int npad = 0;
+  int device = 0;
+  int num_sms = 0;
+  int prec = LJ_PREC_MIXED;
+  bool any_nonperiodic = false;
+
+  // kernel shape / schedule
+  int shape = 0;        // index into kShapes (MIXED)
+  int forced_shape = -1;
+  bool tuned = false;
+  Schedule sched;
+  int BI = 128;
+
+  // device memory
+  DevBuf<double> x, v, f, tf, e, w, stage;
+  DevBuf<int4> q;
+  DevBuf<double4_32a> xd;
+  DevBuf<BlockInfo> blocks;
+  DevBuf<int> cta_tile_begin, cta_block, cta_jt, sys_block_first;
+  DevBuf<DevScalars> sc;
+  DevBuf<BoxArgs> dboxes;
+  DevBuf<double> blk_part;
+  DevBuf<float> partial;  // sized in bytes/4 to also hold doubles
+  DevBuf<int> status;
+  DevBuf<DevRecord> records;
+  DevBuf<unsigned long long> hist;
+  int rec_cap = 0;
+
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+
+  std::map<int, GraphEntry> graphs;
+  std::vector<cudaEvent_t> graph_events;  // placeholders captured into profiled graphs
+
+  // profiling
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  long long prof_steps = 0, prof_pairs = 0;
+  double prof_step_ms = 0, prof_pair_ms = 0;
+
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+lj_status fail(lj_system* s, lj_status code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (s) s->err = buf;
+  else g_create_error = buf;
+  return code;
+}
+
+#define LJ_CUDA(sys, call)                                                                      \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return fail(sys, e_ == cudaErrorMemoryAllocation ? LJ_ERR_OUT_OF_MEMORY : LJ_ERR_CUDA,    \
+                  "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+StateArgs state_args(lj_system* s) {
+  StateArgs a{};
+  a.x = s->x.p;
+  a.v = s->v.p;
+  a.f = s->f.p;
+  a.tf = s->tf.p;
+  a.e = s->e.p;
+  a.w = s->w.p;
+  a.q = s->q.p;
+  a.xd = s->xd.p;
+  a.npad = s->npad;
+  a.blocks = s->blocks.p;
+  a.boxes = s->dboxes.p;
+  a.sc = s->sc.p;
+  a.sys_block_first = s->sys_block_first.p;
+  a.blk_part = s->blk_part.p;
+  a.partial = s->partial.p;
+  a.prec = s->prec;
+  a.bi_threads = s->BI;
+  a.records = s->records.p;
+  a.rec_stride = s->rec_cap;
+  a.status = s->status.p;
+  return a;
+}
+
+PairArgs pair_args(lj_system* s) {
+  PairArgs a{};
+  a.q = s->q.p;
+  a.xd = s->xd.p;
+  a.blocks = s->blocks.p;
+  a.cta_tile_begin = s->cta_tile_begin.p;
+  a.cta_block = s->cta_block.p;
+  a.cta_jt = s->cta_jt.p;
+  a.sc = s->sc.p;
+  a.boxes = s->dboxes.p;
+  a.partial = s->partial.p;
+  a.status = s->status.p;
+  a.hist = HistArgs{0, 1, 1.0f, 0.0f, nullptr};
+  return a;
+}
+
+int nblocks(const lj_system* s) { return (int)s->sched.blocks.size(); }
+
+void clear_graphs(lj_system* s) {
+  for (auto& kv : s->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  s->graphs.clear();
+  for (auto e : s->graph_events) cudaEventDestroy(e);
+  s->graph_events.clear();
+}
+
+lj_status validate(const lj_config* c, lj_system* s) {
+  if (!c) return fail(s, LJ_ERR_INVALID, "config is NULL");
+  if (c->n < 2) return fail(s, LJ_ERR_INVALID, "n must be >= 2 (got %d)", c->n);
+  if (!(c->density > 0) || !std::isfinite(c->density)) return fail(s, LJ_ERR_INVALID, "density must be > 0");
+  if (!(c->temperature >= 0) || !std::isfinite(c->temperature))
+    return fail(s, LJ_ERR_INVALID, "temperature must be >= 0");
+  if (c->boundary < 0 || c->boundary > 2) return fail(s, LJ_ERR_INVALID, "boundary must be 0, 1 or 2");
+  if (c->precision != LJ_PREC_MIXED && c->precision != LJ_PREC_FP64)
+    return fail(s, LJ_ERR_INVALID, "precision must be LJ_PREC_MIXED or LJ_PREC_FP64");
+  if (!(c->epsilon > 0) || !(c->sigma > 0)) return fail(s, LJ_ERR_INVALID, "epsilon and sigma must be > 0");
+  if (c->lattice != LJ_LATTICE_SC && c->lattice != LJ_LATTICE_FCC)
+    return fail(s, LJ_ERR_INVALID, "lattice must be LJ_LATTICE_SC or LJ_LATTICE_FCC");
+  if (!(c->jitter >= 0)) return fail(s, LJ_ERR_INVALID, "jitter must be >= 0");
+  return LJ_OK;
+}
+
+BoxArgs box_args(const lj_config& c) {
+  BoxArgs b{};
+  b.N = c.n;
+  b.bc = c.boundary;
+  b.canonical = c.canonical ? 1 : 0;
+  b.L = std::cbrt((double)c.n / c.density);
+  b.invL = 1.0 / b.L;
+  b.eps = c.epsilon;
+  b.sigma = c.sigma;
+  b.dt = 0.0;
+  b.T0 = c.temperature;
+  b.rho = c.density;
+  return b;
+}
+
+lj_status upload_boxes(lj_system* s) {
+  s->any_nonperiodic = false;
+  for (auto& b : s->boxes) s->any_nonperiodic |= (b.bc != 0);
+  LJ_CUDA(s, cudaMemcpyAsync(s->dboxes.p, s->boxes.data(), sizeof(BoxArgs) * s->nsys, cudaMemcpyHostToDevice,
+                             s->stream));
+  return LJ_OK;
+}
+
+// Builds the stream-K schedule for the active shape and uploads its tables.
+lj_status setup_schedule(lj_system* s) {
+  int threads, tile, blocks_per_sm = 0;
+  if (s->prec == LJ_PREC_FP64) {
+    threads = fp64_block_threads();
+    tile = fp64_tile();
+  } else {
+    threads = kShapes[s->shape].threads;
+    tile = kShapes[s->shape].tile;
+  }
+  LJ_CUDA(s, pair_occupancy(s->prec, s->shape, &blocks_per_sm));
+  if (blocks_per_sm < 1) return fail(s, LJ_ERR_NO_DEVICE, "pair kernel cannot be resident on this device");
+  std::vector<int> n(s->nsys);
+  for (int k = 0; k < s->nsys; ++k) n[k] = s->cfg[k].n;
+  Schedule sch;
+  if (!build_schedule(n.data(), s->nsys, threads, tile, s->num_sms * blocks_per_sm, kTileOverhead, &sch))
+    return fail(s, LJ_ERR_INVALID, "cannot build the pair schedule");
+  s->sched = std::move(sch);
+  s->BI = threads;
+  const int nb = nblocks(s);
+  LJ_CUDA(s, s->blocks.alloc(nb));
+  LJ_CUDA(s, s->cta_tile_begin.alloc(s->sched.G + 1));
+  LJ_CUDA(s, s->cta_block.alloc(s->sched.G));
+  LJ_CUDA(s, s->cta_jt.alloc(s->sched.G));
+  LJ_CUDA(s, s->sys_block_first.alloc(s->nsys + 1));
+  LJ_CUDA(s, s->blk_part.alloc((size_t)nb * 8));
+  // partial: nseg x 5 x BI values of 8 bytes (FP64) or 4 bytes (MIXED)
+  const size_t vals = (size_t)s->sched.nseg * 5 * threads;
+  LJ_CUDA(s, s->partial.alloc(vals * (s->prec == LJ_PREC_FP64 ? 2 : 1)));
+  LJ_CUDA(s, cudaMemcpyAsync(s->blocks.p, s->sched.blocks.data(), sizeof(BlockInfo) * nb, cudaMemcpyHostToDevice,
+                             s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(s->cta_tile_begin.p, s->sched.cta_tile_begin.data(), sizeof(int) * (s->sched.G + 1),
+                             cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(s->cta_block.p, s->sched.cta_block.data(), sizeof(int) * s->sched.G,
+                             cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(s->cta_jt.p, s->sched.cta_jt.data(), sizeof(int) * s->sched.G, cudaMemcpyHostToDevice,
+                             s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(s->sys_block_first.p, s->sched.sys_block_first.data(), sizeof(int) * (s->nsys + 1),
+                             cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  clear_graphs(s);
+  return LJ_OK;
+}
+
+// ---- kernel sequences ----------------------------------------------------
+
+lj_status enqueue_frame_all(lj_system* s) {
+  StateArgs a = state_args(s);
+  const int nb = nblocks(s);
+  LJ_CUDA(s, launch_bbox(a, nb, s->BI, s->stream));
+  LJ_CUDA(s, launch_frame(a, s->nsys, false, s->stream));
+  LJ_CUDA(s, launch_quantize(a, nb, s->BI, false, s->stream));
+  s->launches += 3;
+  return LJ_OK;
+}
+
+lj_status enqueue_pairs(lj_system* s, bool forces, bool hist, const HistArgs* h) {
+  PairArgs p = pair_args(s);
+  if (h) p.hist = *h;
+  LJ_CUDA(s, launch_pairs(s->prec, s->shape, forces, hist, p, s->sched.G, s->stream));
+  s->launches += 1;
+  return LJ_OK;
+}
+
+// Force evaluation + observables at the current positions (CalculateForces +
+// CalculateParameters).
+lj_status enqueue_compute_forces(lj_system* s) {
+  lj_status st = enqueue_frame_all(s);
+  if (st) return st;
+  st = enqueue_pairs(s, true, false, nullptr);
+  if (st) return st;
+  StateArgs a = state_args(s);
+  LJ_CUDA(s, launch_reduce(a, nblocks(s), s->BI, MODE_FORCES_ONLY, s->stream));
+  LJ_CUDA(s, launch_observables(a, s->nsys, MODE_FORCES_ONLY, s->stream));
+  s->launches += 2;
+  return LJ_OK;
+}
+
+cudaEvent_t next_event(lj_system* s) {
+  if (s->ev_used == s->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    s->ev_pool.push_back(e);
+  }
+  return s->ev_pool[s->ev_used++];
+}
+
+// The kernels of one Verlet step, enqueued on s->stream (captured or not).
+// ev (optional): events recorded at step start, pair start, pair end, step end.
+lj_status enqueue_step(lj_system* s, int mode, cudaEvent_t* ev, bool capture, int* kernels) {
+  StateArgs a = state_args(s);
+  const int nb = nblocks(s);
+  int k = 0;
+  const unsigned flags = capture ? cudaEventRecordExternal : cudaEventRecordDefault;
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[0], s->stream, flags));
+  LJ_CUDA(s, launch_drift_mode(a, nb, s->BI, mode, s->stream));
+  ++k;
+  if (s->any_nonperiodic) {
+    LJ_CUDA(s, launch_frame(a, s->nsys, true, s->stream));
+    LJ_CUDA(s, launch_quantize(a, nb, s->BI, true, s->stream));
+    k += 2;
+  }
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[1], s->stream, flags));
+  {
+    PairArgs p = pair_args(s);
+    LJ_CUDA(s, launch_pairs(s->prec, s->shape, true, false, p, s->sched.G, s->stream));
+    ++k;
+  }
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[2], s->stream, flags));
+  LJ_CUDA(s, launch_reduce(a, nb, s->BI, mode, s->stream));
+  ++k;
+  if (mode == MODE_TVN) {
+    LJ_CUDA(s, launch_tvn_finish(a, nb, s->BI, s->stream));
+    ++k;
+  }
+  LJ_CUDA(s, launch_observables(a, s->nsys, mode, s->stream));
+  ++k;
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[3], s->stream, flags));
+  if (kernels) *kernels = k;
+  return LJ_OK;
+}
+
+int step_mode(const lj_system* s) {
+  // A batch with mixed ensembles steps every box with its own flag inside the
+  // kernels; the launch sequence only needs to know whether any box is TVN.
+  for (const auto& b : s->boxes)
+    if (b.canonical) return MODE_TVN;
+  return MODE_EVN;
+}
+
+lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
+  const int key = mode * 4 + (s->any_nonperiodic ? 2 : 0) + (s->profiling ? 1 : 0);
+  auto it = s->graphs.find(key);
+  if (it != s->graphs.end()) {
+    *out = &it->second;
+    return LJ_OK;
+  }
+  GraphEntry ge;
+  ge.profiled = s->profiling;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (ge.profiled)
+    for (auto& e : ev) {
+      LJ_CUDA(s, cudaEventCreate(&e));
+    }
+  cudaGraph_t g = nullptr;
+  LJ_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  lj_status st = enqueue_step(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels);
+  cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+  if (st) return st;
+  LJ_CUDA(s, ce);
+  if (ge.profiled) {
+    size_t nn = 0;
+    LJ_CUDA(s, cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    LJ_CUDA(s, cudaGraphGetNodes(g, nodes.data(), &nn));
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      LJ_CUDA(s, cudaGraphNodeGetType(nd, &t));
+      if (t != cudaGraphNodeTypeEventRecord) continue;
+      cudaEvent_t e;
+      LJ_CUDA(s, cudaGraphEventRecordNodeGetEvent(nd, &e));
+      for (int k = 0; k < 4; ++k)
+        if (e == ev[k]) ge.ev_nodes[k] = nd;
+    }
+  }
+  LJ_CUDA(s, cudaGraphInstantiate(&ge.exec, g, 0));
+  cudaGraphDestroy(g);
+  // The capture-time events stay alive with the graph; before every launch
+  // the nodes are pointed at fresh events from the pool.
+  for (auto& e : ev)
+    if (e) s->graph_events.push_back(e);
+  auto res = s->graphs.emplace(key, ge);
+  *out = &res.first->second;
+  return LJ_OK;
+}
+
+lj_status check_status(lj_system* s) {
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  int st = 0;
+  LJ_CUDA(s, cudaMemcpy(&st, s->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st) {
+    LJ_CUDA(s, cudaMemset(s->status.p, 0, sizeof(int)));
+    if (st & LJ_DEVFLAG_TIMEOUT)
+      return fail(s, LJ_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the results of that launch are void");
+    if (st & LJ_DEVFLAG_NONFINITE)
+      return fail(s, LJ_ERR_NONFINITE, "an observable became NaN/Inf (overlapping particles or blow-up)");
+  }
+  return LJ_OK;
+}
+
+lj_status alloc_state(lj_system* s) {
+  s->npad = (s->ntotal + 255) / 256 * 256;
+  const size_t n3 = 3 * (size_t)s->npad;
+  LJ_CUDA(s, s->x.alloc(n3));
+  LJ_CUDA(s, s->v.alloc(n3));
+  LJ_CUDA(s, s->f.alloc(n3));
+  LJ_CUDA(s, s->tf.alloc(n3));
+  LJ_CUDA(s, s->stage.alloc(n3));
+  LJ_CUDA(s, s->e.alloc(s->npad));
+  LJ_CUDA(s, s->w.alloc(s->npad));
+  LJ_CUDA(s, s->q.alloc(s->npad));
+  LJ_CUDA(s, s->xd.alloc(s->npad));
+  LJ_CUDA(s, s->sc.alloc(s->nsys));
+  LJ_CUDA(s, s->dboxes.alloc(s->nsys));
+  LJ_CUDA(s, s->status.alloc(1));
+  LJ_CUDA(s, s->hist.alloc(kMaxHistBins));
+  LJ_CUDA(s, cudaMemsetAsync(s->x.p, 0, sizeof(double) * n3, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->v.p, 0, sizeof(double) * n3, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->f.p, 0, sizeof(double) * n3, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->tf.p, 0, sizeof(double) * n3, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->q.p, 0, sizeof(int4) * s->npad, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->xd.p, 0, sizeof(double4_32a) * s->npad, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->sc.p, 0, sizeof(DevScalars) * s->nsys, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->status.p, 0, sizeof(int), s->stream));
+  return LJ_OK;
+}
+
+// Uploads an interleaved (N,3) host array of all boxes: one host->device copy
+// into the staging buffer (direct DMA when the caller's buffer is pinned, see
+// lj_host_alloc), then a device transpose into component-major storage.
+lj_status upload_xyz(lj_system* s, const double* host, double* dev) {
+  const size_t bytes = sizeof(double) * 3 * (size_t)s->ntotal;
+  LJ_CUDA(s, cudaMemcpyAsync(s->stage.p, host, bytes, cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, launch_unpack(s->stage.p, dev, s->ntotal, s->npad, s->stream));
+  s->launches += 1;
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LJ_OK;
+}
+
+lj_status download_xyz(lj_system* s, const double* dev, double* host) {
+  const size_t bytes = sizeof(double) * 3 * (size_t)s->ntotal;
+  LJ_CUDA(s, launch_pack(dev, s->stage.p, s->ntotal, s->npad, s->stream));
+  s->launches += 1;
+  LJ_CUDA(s, cudaMemcpyAsync(host, s->stage.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LJ_OK;
+}
+
+lj_status read_scalars(lj_system* s, std::vector<DevScalars>& out) {
+  out.resize(s->nsys);
+  LJ_CUDA(s, cudaMemcpyAsync(out.data(), s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LJ_OK;
+}
+
+lj_status write_scalars(lj_system* s, const std::vector<DevScalars>& in) {
+  LJ_CUDA(s, cudaMemcpyAsync(s->sc.p, in.data(), sizeof(DevScalars) * s->nsys, cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LJ_OK;
+}
+
+void fill_obs(const DevScalars& d, lj_observables* o) {
+  o->t = d.t;
+  o->K = d.K;
+  o->V = d.V;
+  o->T = d.T;
+  o->P = d.P_press;
+  o->U = d.U;
+  o->W = d.W;
+  o->Pshear = d.Pshear;
+  o->Tkin_tvn = d.Tkin;
+  o->av_U_tot = d.av_U;
+  o->av_T_tot = d.av_T;
+  o->av_p_tot = d.av_p;
+  o->av_iters = d.av_iters;
+  o->step = d.step;
+}
+
+// Creates the handle for `nsys` boxes (a batch when nsys > 1); the initial
+// state of every box is sampled from its own config.
+lj_status create_impl(const lj_config* cfgs, int nsys, lj_system** out) {
+  if (!out) return fail(nullptr, LJ_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!cfgs || nsys < 1) return fail(nullptr, LJ_ERR_INVALID, "no configuration");
+  for (int k = 0; k < nsys; ++k) {
+    lj_status st = validate(&cfgs[k], nullptr);
+    if (st) return st;
+    if (cfgs[k].precision != cfgs[0].precision || cfgs[k].device != cfgs[0].device ||
+        (cfgs[k].canonical != 0) != (cfgs[0].canonical != 0))
+      return fail(nullptr, LJ_ERR_INVALID, "all boxes of a batch must share precision, device and ensemble");
+  }
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev == 0)
+    return fail(nullptr, LJ_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(ce));
+  if (cfgs[0].device < 0 || cfgs[0].device >= ndev)
+    return fail(nullptr, LJ_ERR_INVALID, "device %d out of range (%d devices)", cfgs[0].device, ndev);
+  cudaDeviceProp prop;
+  ce = cudaGetDeviceProperties(&prop, cfgs[0].device);
+  if (ce != cudaSuccess) return fail(nullptr, LJ_ERR_NO_DEVICE, "%s", cudaGetErrorString(ce));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(nullptr, LJ_ERR_NO_DEVICE, "device %s is sm_%d%d; this library is built for sm_103a only",
+                prop.name, prop.major, prop.minor);
+  long long total = 0;
+  for (int k = 0; k < nsys; ++k) total += cfgs[k].n;
+  if (total > (1ll << 30)) return fail(nullptr, LJ_ERR_INVALID, "too many particles (%lld)", total);
+
+  lj_system* s = new lj_system();
+  s->nsys = nsys;
+  s->cfg.assign(cfgs, cfgs + nsys);
+  s->ntotal = (int)total;
+  s->device = cfgs[0].device;
+  s->num_sms = prop.multiProcessorCount;
+  s->prec = cfgs[0].precision;
+  for (int k = 0; k < nsys; ++k) s->boxes.push_back(box_args(cfgs[k]));
+  auto bail = [&](lj_status st) {
+    g_create_error = s->err;
+    lj_destroy(s);
+    return st;
+  };
+  if (cudaSetDevice(s->device) != cudaSuccess) return bail(fail(s, LJ_ERR_CUDA, "cudaSetDevice failed"));
+  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(s, LJ_ERR_CUDA, "cudaStreamCreate failed"));
+  s->stream = s->own_stream;
+  lj_status st = alloc_state(s);
+  if (st) return bail(st);
+  st = upload_boxes(s);
+  if (st) return bail(st);
+  // Shape: the reference's CUDABlockSize picks the nearest i-block size.
+  s->shape = 0;
+  if (cfgs[0].block_hint > 0 && s->prec == LJ_PREC_MIXED) {
+    int best = 0;
+    for (int k = 0; k < kNumShapes; ++k)
+      if (std::abs(kShapes[k].threads - cfgs[0].block_hint) < std::abs(kShapes[best].threads - cfgs[0].block_hint))
+        best = k;
+    s->shape = best;
+    s->forced_shape = best;
+  }
+  st = setup_schedule(s);
+  if (st) return bail(st);
+  // Initial state (host sampler), then forces and observables on the device.
+  std::vector<double> pos(3 * (size_t)s->ntotal), vel(3 * (size_t)s->ntotal);
+  size_t off = 0;
+  for (int k = 0; k < nsys; ++k) {
+    const lj_config& c = cfgs[k];
+    if (!sample_initial_state(c.n, s->boxes[k].L, c.temperature, c.lattice, c.jitter, c.sigma, c.seed,
+                              pos.data() + 3 * off, vel.data() + 3 * off))
+      return bail(fail(s, LJ_ERR_INVALID, "initial-state sampling failed for box %d", k));
+    off += c.n;
+  }
+  st = upload_xyz(s, pos.data(), s->x.p);
+  if (st) return bail(st);
+  st = upload_xyz(s, vel.data(), s->v.p);
+  if (st) return bail(st);
+  st = enqueue_compute_forces(s);
+  if (st) return bail(st);
+  st = check_status(s);
+  if (st) return bail(st);
+  // Reinitialize resets the averages after its CalculateParameters (MDSystem.cpp:112-113).
+  std::vector<DevScalars> sc;
+  st = read_scalars(s, sc);
+  if (st) return bail(st);
+  for (auto& d : sc) {
+    d.av_U = d.av_T = d.av_p = 0.0;
+    d.av_iters = 0;
+  }
+  st = write_scalars(s, sc);
+  if (st) return bail(st);
+  *out = s;
+  return LJ_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+lj_status lj_config_default(lj_config* c) {
+  if (!c) return LJ_ERR_INVALID;
+  std::memset(c, 0, sizeof(*c));
+  c->n = 128;
+  c->temperature = 1.5;
+  c->density = 0.2;
+  c->canonical = 0;
+  c->boundary = LJ_BC_PERIODIC;
+  c->precision = LJ_PREC_MIXED;
+  c->epsilon = 1.0;
+  c->sigma = 1.0;
+  c->lattice = LJ_LATTICE_SC;
+  c->jitter = 0.0;
+  c->seed = 1;
+  c->block_hint = 0;
+  c->device = 0;
+  c->autotune = 1;
+  return LJ_OK;
+}
+
+lj_status lj_create(const lj_config* cfg, lj_system** out) { return create_impl(cfg, 1, out); }
+
+lj_status lj_batch_create(const lj_config* cfgs, int32_t nsys, lj_system** out) {
+  return create_impl(cfgs, nsys, out);
+}
+
+lj_status lj_destroy(lj_system* s) {
+  if (!s) return LJ_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  clear_graphs(s);
+  for (auto e : s->ev_pool) cudaEventDestroy(e);
+  s->x.free();
+  s->v.free();
+  s->f.free();
+  s->tf.free();
+  s->e.free();
+  s->w.free();
+  s->stage.free();
+  s->q.free();
+  s->xd.free();
+  s->blocks.free();
+  s->cta_tile_begin.free();
+  s->cta_block.free();
+  s->cta_jt.free();
+  s->sys_block_first.free();
+  s->sc.free();
+  s->dboxes.free();
+  s->blk_part.free();
+  s->partial.free();
+  s->status.free();
+  s->records.free();
+  s->hist.free();
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+  return LJ_OK;
+}
+
+const char* lj_last_error(const lj_system* s) { return s ? s->err.c_str() : g_create_error.c_str(); }
+
+lj_status lj_get_info(const lj_system* s, int32_t* n, double* box) {
+  if (!s) return LJ_ERR_INVALID;
+  if (n) *n = s->cfg[0].n;
+  if (box) *box = s->boxes[0].L;
+  return LJ_OK;
+}
+
+lj_status lj_reinitialize(lj_system* s, const lj_config* cfg) {
+  if (!s || !cfg) return LJ_ERR_INVALID;
+  if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "lj_reinitialize applies to single-box handles");
+  lj_status st = validate(cfg, s);
+  if (st) return st;
+  lj_system* fresh = nullptr;
+  st = create_impl(cfg, 1, &fresh);
+  if (st) return fail(s, st, "%s", g_create_error.c_str());
+  // Swap the new state into the caller's handle (the handle pointer stays valid).
+  cudaStream_t user_stream = (s->stream != s->own_stream) ? s->stream : nullptr;
+  std::swap(*s, *fresh);
+  lj_destroy(fresh);
+  if (user_stream) s->stream = user_stream;
+  return LJ_OK;
+}
+
+lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  if (pos) {
+    for (size_t k = 0; k < 3 * (size_t)s->ntotal; ++k)
+      if (!std::isfinite(pos[k])) return fail(s, LJ_ERR_INVALID, "position %zu is not finite", k / 3);
+    lj_status st = upload_xyz(s, pos, s->x.p);
+    if (st) return st;
+  }
+  if (vel) {
+    for (size_t k = 0; k < 3 * (size_t)s->ntotal; ++k)
+      if (!std::isfinite(vel[k])) return fail(s, LJ_ERR_INVALID, "velocity %zu is not finite", k / 3);
+    lj_status st = upload_xyz(s, vel, s->v.p);
+    if (st) return st;
+  }
+  return LJ_OK;
+}
+
+lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  if (pos && (st = download_xyz(s, s->x.p, pos))) return st;
+  if (vel && (st = download_xyz(s, s->v.p, vel))) return st;
+  if (force && (st = download_xyz(s, s->f.p, force))) return st;
+  return LJ_OK;
+}
+
+lj_status lj_get_pair_sums(lj_system* s, double* e, double* w) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  if (e) LJ_CUDA(s, cudaMemcpy(e, s->e.p, sizeof(double) * s->ntotal, cudaMemcpyDeviceToHost));
+  if (w) LJ_CUDA(s, cudaMemcpy(w, s->w.p, sizeof(double) * s->ntotal, cudaMemcpyDeviceToHost));
+  return LJ_OK;
+}
+
+lj_status lj_compute_forces(lj_system* s) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  return enqueue_compute_forces(s);
+}
+
+lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
+  if (!s) return LJ_ERR_INVALID;
+  if (nsteps < 0) return fail(s, LJ_ERR_INVALID, "nsteps must be >= 0");
+  if (!(dt > 0) || !std::isfinite(dt)) return fail(s, LJ_ERR_INVALID, "dt must be > 0");
+  if (nsteps == 0) return LJ_OK;
+  cudaSetDevice(s->device);
+  bool changed = false;
+  for (auto& b : s->boxes)
+    if (b.dt != dt) {
+      b.dt = dt;
+      changed = true;
+    }
+  if (changed) {
+    lj_status st = upload_boxes(s);
+    if (st) return st;
+  }
+  const int mode = step_mode(s);
+  GraphEntry* ge = nullptr;
+  lj_status st = get_graph(s, mode, &ge);
+  if (st) return st;
+  for (int k = 0; k < nsteps; ++k) {
+    if (ge->profiled) {
+      for (int e = 0; e < 4; ++e) {
+        cudaEvent_t ev = next_event(s);
+        if (!ev) return fail(s, LJ_ERR_CUDA, "cudaEventCreate failed");
+        if (ge->ev_nodes[e]) LJ_CUDA(s, cudaGraphExecEventRecordNodeSetEvent(ge->exec, ge->ev_nodes[e], ev));
+      }
+    }
+    LJ_CUDA(s, cudaGraphLaunch(ge->exec, s->stream));
+    s->launches += ge->kernels;
+  }
+  return LJ_OK;
+}
+
+lj_status lj_sync(lj_system* s) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  return check_status(s);
+}
+
+lj_status lj_get_observables(lj_system* s, lj_observables* out) {
+  if (!s || !out) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  std::vector<DevScalars> sc;
+  if ((st = read_scalars(s, sc))) return st;
+  fill_obs(sc[0], out);
+  return LJ_OK;
+}
+
+lj_status lj_batch_observables(lj_system* s, lj_observables* out) {
+  if (!s || !out) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  std::vector<DevScalars> sc;
+  if ((st = read_scalars(s, sc))) return st;
+  for (int k = 0; k < s->nsys; ++k) fill_obs(sc[k], out + k);
+  return LJ_OK;
+}
+
+lj_status lj_set_recording(lj_system* s, int32_t cap) {
+  if (!s || cap < 0) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  LJ_CUDA(s, s->records.alloc((size_t)cap * s->nsys));
+  s->rec_cap = cap;
+  std::vector<DevScalars> sc;
+  lj_status st = read_scalars(s, sc);
+  if (st) return st;
+  for (auto& d : sc) {
+    d.rec_cap = cap;
+    d.rec_count = 0;
+  }
+  clear_graphs(s);  // records pointer / stride are captured
+  return write_scalars(s, sc);
+}
+
+lj_status lj_get_records(lj_system* s, lj_observables* out, int32_t max, int32_t* count) {
+  if (!s || !count || max < 0) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  *count = 0;
+  if (s->rec_cap == 0) return LJ_OK;
+  std::vector<DevScalars> sc;
+  if ((st = read_scalars(s, sc))) return st;
+  std::vector<DevRecord> rec(s->rec_cap);
+  LJ_CUDA(s, cudaMemcpy(rec.data(), s->records.p, sizeof(DevRecord) * s->rec_cap, cudaMemcpyDeviceToHost));
+  const long long total = sc[0].rec_count;
+  const long long have = std::min<long long>(total, s->rec_cap);
+  const long long first = total - have;
+  int n = 0;
+  for (long long k = first; k < total && n < max; ++k, ++n) {
+    const DevRecord& r = rec[k % s->rec_cap];
+    lj_observables& o = out[n];
+    o.t = r.t;
+    o.K = r.K;
+    o.V = r.V;
+    o.T = r.T;
+    o.P = r.P;
+    o.U = r.U;
+    o.W = r.W;
+    o.Pshear = r.Pshear;
+    o.Tkin_tvn = r.Tkin;
+    o.av_U_tot = r.av_U;
+    o.av_T_tot = r.av_T;
+    o.av_p_tot = r.av_p;
+    o.av_iters = r.av_iters;
+    o.step = r.step;
+  }
+  *count = n;
+  return LJ_OK;
+}
+
+lj_status lj_reset_averaging(lj_system* s) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  std::vector<DevScalars> sc;
+  lj_status st = read_scalars(s, sc);
+  if (st) return st;
+  for (auto& d : sc) {
+    d.av_U = d.av_T = d.av_p = 0.0;
+    d.av_iters = 0;
+  }
+  return write_scalars(s, sc);
+}
+
+lj_status lj_set_canonical(lj_system* s, int32_t canonical) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  for (int k = 0; k < s->nsys; ++k) {
+    s->cfg[k].canonical = canonical ? 1 : 0;
+    s->boxes[k].canonical = canonical ? 1 : 0;
+  }
+  return upload_boxes(s);
+}
+
+lj_status lj_set_boundary(lj_system* s, int32_t bc) {
+  if (!s) return LJ_ERR_INVALID;
+  if (bc < 0 || bc > 2) return fail(s, LJ_ERR_INVALID, "boundary must be 0, 1 or 2");
+  cudaSetDevice(s->device);
+  for (int k = 0; k < s->nsys; ++k) {
+    s->cfg[k].boundary = bc;
+    s->boxes[k].bc = bc;
+  }
+  lj_status st = upload_boxes(s);
+  if (st) return st;
+  // The shadow frame depends on the boundary; rebuild it from the positions.
+  return enqueue_frame_all(s);
+}
+
+lj_status lj_set_temperature(lj_system* s, double T0) {
+  if (!s || !(T0 >= 0)) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  for (int k = 0; k < s->nsys; ++k) {
+    s->cfg[k].temperature = T0;
+    s->boxes[k].T0 = T0;
+  }
+  return upload_boxes(s);
+}
+
+lj_status lj_set_time(lj_system* s, double t) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  std::vector<DevScalars> sc;
+  lj_status st = read_scalars(s, sc);
+  if (st) return st;
+  for (auto& d : sc) d.t = t;
+  return write_scalars(s, sc);
+}
+
+lj_status lj_renormalize_velocities(lj_system* s, int32_t recalc) {
+  if (!s) return LJ_ERR_INVALID;
+  if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "renormalization applies to single-box handles");
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  std::vector<DevScalars> sc;
+  if ((st = read_scalars(s, sc))) return st;
+  const double T0 = s->boxes[0].T0, N = s->cfg[0].n;
+  double Tkin = sc[0].T;
+  StateArgs a = state_args(s);
+  if (recalc) {
+    LJ_CUDA(s, launch_scale_velocities(a, nblocks(s), s->BI, 1, 1.0, s->stream));
+    s->launches += 1;
+    std::vector<double> part((size_t)nblocks(s) * 8);
+    LJ_CUDA(s, cudaMemcpyAsync(part.data(), s->blk_part.p, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                               s->stream));
+    LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+    double K = 0;
+    for (int b = 0; b < nblocks(s); ++b) K += part[(size_t)b * 8];
+    Tkin = 2.0 * K / 3.0 / N;  // KineticTemperature = sum v^2/(3N)
+  }
+  if (!(Tkin > 0)) return fail(s, LJ_ERR_INVALID, "kinetic temperature is zero; cannot rescale");
+  LJ_CUDA(s, launch_scale_velocities(a, nblocks(s), s->BI, 0, std::sqrt(T0 / Tkin), s->stream));
+  s->launches += 1;
+  // MDSystem.cpp:386-388: K *= T0/Tkin; T = T0; U = K + V.
+  sc[0].K *= T0 / Tkin;
+  sc[0].T = T0;
+  sc[0].U = sc[0].K + sc[0].V;
+  return write_scalars(s, sc);
+}
+
+lj_status lj_renormalize_velocities_to_energy(lj_system* s, double ust) {
+  if (!s) return LJ_ERR_INVALID;
+  if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "renormalization applies to single-box handles");
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  std::vector<DevScalars> sc;
+  if ((st = read_scalars(s, sc))) return st;
+  const double Kold = sc[0].K;
+  const double Kdes = ust * s->cfg[0].n - sc[0].V;
+  if (!(Kold > 0) || !(Kdes >= 0))
+    return fail(s, LJ_ERR_INVALID, "target energy %.6g per particle is below the potential energy", ust);
+  StateArgs a = state_args(s);
+  LJ_CUDA(s, launch_scale_velocities(a, nblocks(s), s->BI, 0, std::sqrt(Kdes / Kold), s->stream));
+  s->launches += 1;
+  sc[0].K = Kdes;
+  sc[0].U = sc[0].K + sc[0].V;
+  return write_scalars(s, sc);
+}
+
+float lj_reference_rdf_dr2(int32_t n) {
+  // MDSystem.cpp:93-95, with the float member's roundings.
+  if (n < 1) return 0.0f;
+  const double a = 0.2 * std::sqrt(100. / n);
+  float dr2 = (float)(a > 0.05 ? a : 0.05);
+  if (250 * dr2 < 25.0) dr2 = (float)(25.0 / 250);
+  return dr2;
+}
+
+lj_status lj_rdf_counts(lj_system* s, int32_t mode, int32_t nbins, double width, uint64_t* counts) {
+  if (!s || !counts) return LJ_ERR_INVALID;
+  if (mode < 0 || mode > 2) return fail(s, LJ_ERR_INVALID, "unknown RDF mode %d", mode);
+  if (nbins < 1 || nbins > kMaxHistBins) return fail(s, LJ_ERR_INVALID, "nbins must be in [1, %d]", kMaxHistBins);
+  if (!(width > 0)) return fail(s, LJ_ERR_INVALID, "bin width must be > 0");
+  if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "RDF counts apply to single-box handles");
+  cudaSetDevice(s->device);
+  lj_status st = enqueue_frame_all(s);
+  if (st) return st;
+  LJ_CUDA(s, cudaMemsetAsync(s->hist.p, 0, sizeof(unsigned long long) * nbins, s->stream));
+  HistArgs h{};
+  h.mode = mode;
+  h.nb = nbins;
+  const double sig = s->cfg[0].sigma;
+  // bins in reduced units: width / sigma^2 (r^2 bins) or width / sigma (r bins)
+  if (mode == 2) {
+    h.inv_w = (float)(sig / width);
+    const double rmax = nbins * width / sig;
+    h.rmax2 = (float)(rmax * rmax);
+  } else {
+    h.inv_w = (float)(sig * sig / width);
+    h.rmax2 = 0.0f;
+  }
+  h.counts = s->hist.p;
+  // The histogram path always runs on the fixed-point shadow.
+  const int saved = s->prec;
+  s->prec = LJ_PREC_MIXED;
+  PairArgs p = pair_args(s);
+  p.hist = h;
+  // FP64 handles schedule 128-particle i-blocks and 256-record j-tiles,
+  // the geometry of MIXED shape 0, so that shape reads their tables.
+  const int shape = (saved == LJ_PREC_MIXED) ? s->shape : 0;
+  const cudaError_t ce = launch_pairs(LJ_PREC_MIXED, shape, false, true, p, s->sched.G, s->stream);
+  s->prec = saved;
+  LJ_CUDA(s, ce);
+  s->launches += 1;
+  LJ_CUDA(s, cudaMemcpyAsync(counts, s->hist.p, sizeof(unsigned long long) * nbins, cudaMemcpyDeviceToHost,
+                             s->stream));
+  return check_status(s);
+}
+
+lj_status lj_velocity_counts(lj_system* s, double step, int32_t nbins, uint64_t* counts) {
+  if (!s || !counts) return LJ_ERR_INVALID;
+  if (nbins < 1 || nbins > kMaxHistBins) return fail(s, LJ_ERR_INVALID, "nbins must be in [1, %d]", kMaxHistBins);
+  if (!(step > 0)) return fail(s, LJ_ERR_INVALID, "step must be > 0");
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaMemsetAsync(s->hist.p, 0, sizeof(unsigned long long) * nbins, s->stream));
+  StateArgs a = state_args(s);
+  LJ_CUDA(s, launch_velocity_hist(a, nblocks(s), s->BI, step, nbins, s->hist.p, s->stream));
+  s->launches += 1;
+  LJ_CUDA(s, cudaMemcpyAsync(counts, s->hist.p, sizeof(unsigned long long) * nbins, cudaMemcpyDeviceToHost,
+                             s->stream));
+  return check_status(s);
+}
+
+lj_status lj_tune_info(lj_system* s, int32_t* nshapes, int32_t* active, int32_t k, int32_t* threads, int32_t* ipt,
+                       int32_t* tile) {
+  if (!s) return LJ_ERR_INVALID;
+  if (nshapes) *nshapes = kNumShapes;
+  if (active) *active = s->shape;
+  if (k >= 0 && k < kNumShapes) {
+    if (threads) *threads = kShapes[k].threads;
+    if (ipt) *ipt = 1;
+    if (tile) *tile = kShapes[k].tile;
+  }
+  return LJ_OK;
+}
+
+lj_status lj_set_kernel_shape(lj_system* s, int32_t shape) {
+  if (!s) return LJ_ERR_INVALID;
+  if (shape < -1 || shape >= kNumShapes) return fail(s, LJ_ERR_INVALID, "shape %d out of range", shape);
+  if (s->prec == LJ_PREC_FP64) return LJ_OK;  // one FP64 shape
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->forced_shape = shape;
+  s->shape = shape < 0 ? 0 : shape;
+  lj_status st = setup_schedule(s);
+  if (st) return st;
+  // The i-block length changed: rebuild shadows and the per-block sums.
+  return enqueue_compute_forces(s);
+}
+
+lj_status lj_autotune(lj_system* s) {
+  if (!s) return LJ_ERR_INVALID;
+  if (s->prec == LJ_PREC_FP64) return LJ_OK;
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  cudaEvent_t e0, e1;
+  LJ_CUDA(s, cudaEventCreate(&e0));
+  LJ_CUDA(s, cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 1e30f;
+  for (int k = 0; k < kNumShapes; ++k) {
+    s->shape = k;
+    lj_status st = setup_schedule(s);
+    if (st) return st;
+    if ((st = enqueue_frame_all(s))) return st;
+    for (int w = 0; w < 2; ++w)
+      if ((st = enqueue_pairs(s, true, false, nullptr))) return st;
+    LJ_CUDA(s, cudaEventRecord(e0, s->stream));
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r)
+      if ((st = enqueue_pairs(s, true, false, nullptr))) return st;
+    LJ_CUDA(s, cudaEventRecord(e1, s->stream));
+    LJ_CUDA(s, cudaEventSynchronize(e1));
+    float ms = 0;
+    LJ_CUDA(s, cudaEventElapsedTime(&ms, e0, e1));
+    if ((st = check_status(s))) return st;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = k;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->shape = best;
+  s->tuned = true;
+  lj_status st = setup_schedule(s);
+  if (st) return st;
+  return enqueue_compute_forces(s);
+}
+
+lj_status lj_profile_enable(lj_system* s, int32_t on) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->profiling = on != 0;
+  s->ev_used = 0;
+  s->prof_steps = s->prof_pairs = 0;
+  s->prof_step_ms = s->prof_pair_ms = 0;
+  return LJ_OK;
+}
+
+lj_status lj_profile_read(lj_system* s, int64_t* pair_launches, double* pair_ms, int64_t* steps, double* step_ms) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  // Events are used four per step: step start, pair start, pair end, step end.
+  for (size_t k = 0; k + 3 < s->ev_used; k += 4) {
+    float a = 0, b = 0;
+    LJ_CUDA(s, cudaEventElapsedTime(&a, s->ev_pool[k + 1], s->ev_pool[k + 2]));
+    LJ_CUDA(s, cudaEventElapsedTime(&b, s->ev_pool[k], s->ev_pool[k + 3]));
+    s->prof_pair_ms += a;
+    s->prof_step_ms += b;
+    s->prof_pairs += 1;
+    s->prof_steps += 1;
+  }
+  s->ev_used = 0;
+  if (pair_launches) *pair_launches = s->prof_pairs;
+  if (pair_ms) *pair_ms = s->prof_pair_ms;
+  if (steps) *steps = s->prof_steps;
+  if (step_ms) *step_ms = s->prof_step_ms;
+  return LJ_OK;
+}
+
+lj_status lj_get_stream(lj_system* s, void** stream) {
+  if (!s || !stream) return LJ_ERR_INVALID;
+  *stream = (void*)s->stream;
+  return LJ_OK;
+}
+
+lj_status lj_set_stream(lj_system* s, void* stream) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  clear_graphs(s);
+  return LJ_OK;
+}
+
+int64_t lj_kernel_launch_count(const lj_system* s) { return s ? s->launches : 0; }
+
+lj_status lj_batch_info(const lj_system* s, int32_t* nsys, int32_t* offsets) {
+  if (!s) return LJ_ERR_INVALID;
+  if (nsys) *nsys = s->nsys;
+  if (offsets) {
+    int32_t o = 0;
+    for (int k = 0; k < s->nsys; ++k) {
+      offsets[k] = o;
+      o += s->cfg[k].n;
+    }
+    offsets[s->nsys] = o;
+  }
+  return LJ_OK;
+}
+
+const char* lj_version(void) { return "lj_gb300 1.0 (sm_103a)"; }
+
+void* lj_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (bytes == 0 || cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void lj_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+lj_status lj_sample_initial_state(const lj_config* cfg, double* pos, double* vel) {
+  lj_status st = validate(cfg, nullptr);
+  if (st) return st;
+  if (!pos || !vel) return fail(nullptr, LJ_ERR_INVALID, "pos and vel must be non-NULL");
+  const double L = std::cbrt((double)cfg->n / cfg->density);
+  if (!sample_initial_state(cfg->n, L, cfg->temperature, cfg->lattice, cfg->jitter, cfg->sigma, cfg->seed, pos, vel))
+    return fail(nullptr, LJ_ERR_INVALID, "initial-state sampling failed");
+  return LJ_OK;
+}
+
+lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_t tile, int32_t ctas,
+                           int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin, int32_t* block_info,
+                           int32_t max_blocks) {
+  Schedule sch;
+  if (!build_schedule(n, nsys, block, tile, ctas, kTileOverhead, &sch))
+    return fail(nullptr, LJ_ERR_INVALID, "invalid schedule request");
+  if (out_ctas) *out_ctas = sch.G;
+  if (out_nseg) *out_nseg = sch.nseg;
+  if (cta_tile_begin)
+    for (int g = 0; g <= sch.G; ++g) cta_tile_begin[g] = sch.cta_tile_begin[g];
+  if (block_info) {
+    const int nb = std::min<int>(max_blocks, (int)sch.blocks.size());
+    for (int b = 0; b < nb; ++b) {
+      const BlockInfo& bi = sch.blocks[b];
+      int32_t* o = block_info + 8 * b;
+      o[0] = bi.sys;
+      o[1] = bi.i0;
+      o[2] = bi.n_i;
+      o[3] = bi.p0;
+      o[4] = bi.njt;
+      o[5] = bi.seg_first;
+      o[6] = bi.seg_count;
+      o[7] = bi.g_first;
+    }
+  }
+  return LJ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+"""In-tree build of liblj_gb300.so for sm_103a.
+
+Each translation unit is compiled by nvcc in parallel (one -gencode, no
+cmake), then linked into a shared library next to this package:
+lennard-jones-cuda_gb300/liblj_gb300.so.  The library exports the C ABI of
+include/lj_gb300.h and include/lj_reference_abi.h.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))  # lennard-jones-cuda_gb300/
+REPO = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+INCLUDE = os.path.join(REPO, "include")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+LIB_PATH = os.path.join(PKG_DIR, "liblj_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = [
+    "lj_pairs.cu",
+    "lj_integrate.cu",
+    "lj_compat.cu",
+    "lj_system.cpp",
+    "lj_schedule.cpp",
+    "lj_init.cpp",
+    "MDSystem.cpp",
+]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _flags():
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE, "-I", CSRC,
+                   "-Xptxas", "-warn-spills"]
+
+
+def _compile(src: str, verbose: bool) -> str:
+    obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+    cmd = [nvcc()] + _flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
+    if verbose:
+        cmd += ["-Xptxas", "-v"] if src.endswith(".cu") else []
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
+    if verbose and r.stderr:
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    for d in (CSRC, INCLUDE):
+        for root, _, files in os.walk(d):
+            for f in files:
+                if os.path.getmtime(os.path.join(root, f)) > t:
+                    return True
+    return os.path.getmtime(os.path.abspath(__file__)) > t
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile the CUDA/C++ sources into liblj_gb300.so (skipped when fresh)."""
+    if not force and not _stale():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    tmp = LIB_PATH + ".tmp"
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,169 @@
+"""Integrator, boundaries, observables and running averages (GPU tests).
+
+Step-by-step parity of the device velocity Verlet (EVN) and constant-kinetic-
+temperature Verlet (TVN) with the FP64 oracle restatement of
+MDSystem::Integrate (MDSystem.cpp:438-583), on identical seeded states,
+through the C ABI.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import lj_testutil as U
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def run_pair(ljgb, oracle_mod, pos, vel, N, rho, T0, canonical, bc, dt, steps, prec):
+    s = ljgb.System(n=N, density=rho, temperature=T0, boundary=bc, canonical=int(canonical), precision=prec)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    o = oracle_mod.F64System(pos, vel, s.L, rho, T0, canonical, bc, nthreads=4)
+    for k in range(steps):
+        s.integrate(dt)
+        o.step(dt)
+    p, v, f = s.get_state()
+    return s, o, p, v, f
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["mixed", "fp64"])
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_trajectory_matches_fp64_oracle(ljgb_mod, oracle_mod, path, prec):
+    g = dict(np.load(path))
+    N, rho, T0, bc = int(g["N"]), float(g["rho"]), float(g["T0"]), int(g["bc"])
+    pos = g["pos0"][:, :3].astype(np.float64)
+    vel = g["vel0"][:, :3].astype(np.float64)
+    steps = 20
+    s, o, p, v, f = run_pair(ljgb_mod, oracle_mod, pos, vel, N, rho, T0, bool(g["canonical"]), bc,
+                             float(g["dt"]), steps, prec)
+    tol = 1e-7 if prec == 0 else 1e-11
+    assert np.abs(p - o.pos).max() < tol * max(1.0, s.L)
+    assert np.abs(v - o.vel).max() < tol * 10
+    obs = s.observables()
+    for k in ("K", "V", "T", "P", "U"):
+        assert obs[k] == pytest.approx(getattr(o, k), rel=tol * 10, abs=tol * 10 * N), k
+    assert obs["t"] == pytest.approx(o.t, rel=1e-14)
+    assert obs["step"] == steps
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["mixed", "fp64"])
+def test_tvn_dense_liquid(ljgb_mod, oracle_mod, prec):
+    N, rho, T0 = 2048, 0.85, 1.0
+    pos, vel, L = U.lattice_state(N, rho, 1.3, "fcc", 0.02, seed=3)
+    s, o, p, v, f = run_pair(ljgb_mod, oracle_mod, pos, vel, N, rho, T0, True, 0, 0.005, 10, prec)
+    obs = s.observables()
+    assert np.abs(v - o.vel).max() < (1e-7 if prec == 0 else 1e-11)
+    # the TVN scale was computed from the half-kicked velocities
+    assert obs["Tkin_tvn"] > 0
+    assert obs["T"] == pytest.approx(o.T, rel=1e-8)
+
+
+def test_records_and_time(ljgb_mod):
+    N, rho = 400, 0.05
+    pos, vel, L = U.lattice_state(N, rho, 1.4, "sc", 0.05, seed=1)
+    s = ljgb_mod.System(n=N, density=rho, temperature=1.4)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    s.set_recording(64)
+    s.integrate(0.005, 100)
+    rec = s.records()
+    assert len(rec) == 64
+    steps = [r["step"] for r in rec]
+    assert steps == list(range(37, 101))
+    assert rec[-1]["t"] == pytest.approx(100 * 0.005)
+    obs = s.observables()
+    assert obs["U"] == rec[-1]["U"] and obs["step"] == 100
+    # running averages advance every step (CalculateParameters, MDSystem.cpp:355-358)
+    assert obs["av_iters"] == 101
+    assert rec[-1]["av_U_tot"] == obs["av_U_tot"]
+
+
+def test_energy_conservation_and_momentum(ljgb_mod):
+    """EVN, periodic, config-1 point (N=400, rho=0.05, T=1.4), 2000 steps."""
+    N, rho = 400, 0.05
+    pos, vel, L = U.lattice_state(N, rho, 1.4, "sc", 0.05, seed=1)
+    drift = {}
+    for prec in (0, 1):
+        s = ljgb_mod.System(n=N, density=rho, temperature=1.4, precision=prec)
+        s.set_state(pos, vel)
+        s.calculate_forces()
+        U0 = s.observables()["U"]
+        s.set_recording(2000)
+        s.integrate(0.002, 2000)
+        Us = np.array([r["U"] for r in s.records()])
+        _, v, _ = s.get_state()
+        assert np.abs(v.sum(0)).max() < 1e-9
+        drift[prec] = np.abs(Us - U0).max() / N
+    assert drift[1] < 2e-3
+    assert drift[0] < 2e-3
+    assert abs(drift[0] - drift[1]) < 1e-4
+
+
+def test_wall_keeps_particles_in_box(ljgb_mod):
+    N, rho = 500, 0.3
+    s = ljgb_mod.System(n=N, density=rho, temperature=2.0, boundary=1, jitter=0.05, seed=7)
+    s.integrate(0.005, 400)
+    p, v, _ = s.get_state()
+    assert p.min() > -0.5 and p.max() < s.L + 0.5
+
+
+def test_periodic_wrap(ljgb_mod):
+    N, rho = 300, 0.1
+    s = ljgb_mod.System(n=N, density=rho, temperature=3.0, seed=4)
+    s.integrate(0.005, 300)
+    p, _, _ = s.get_state()
+    assert p.min() >= -1e-9 and p.max() <= s.L + 1e-9
+
+
+def test_renormalize_and_reset(ljgb_mod):
+    s = ljgb_mod.System(n=512, density=0.5, temperature=1.2, seed=3)
+    s.integrate(0.005, 50)
+    s.renormalize_velocities(True)
+    _, v, _ = s.get_state()
+    assert np.sum(v * v) / 3 / 512 == pytest.approx(1.2, rel=1e-12)
+    assert s.observables()["T"] == 1.2
+    o = s.observables()
+    s.renormalize_velocities_to_energy(o["V"] / 512 + 1.0)
+    _, v, _ = s.get_state()
+    assert 0.5 * np.sum(v * v) == pytest.approx(512.0, rel=1e-12)
+    s.reset_averaging()
+    assert s.observables()["av_iters"] == 0
+    s.set_time(3.0)
+    s.integrate(0.01, 2)
+    assert s.observables()["t"] == pytest.approx(3.02)
+
+
+def test_set_canonical_and_boundary_switch(ljgb_mod, oracle_mod):
+    N, rho = 600, 0.4
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "sc", 0.05, seed=12)
+    s = ljgb_mod.System(n=N, density=rho, temperature=1.0)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    o = oracle_mod.F64System(pos, vel, L, rho, 1.0, False, 0, nthreads=4)
+    for k in range(6):
+        s.integrate(0.005)
+        o.step(0.005)
+    s.set_canonical(True)
+    o.canonical = True
+    s.set_boundary(1)
+    o.bc = 1
+    s.calculate_forces()
+    o.compute_forces()
+    for k in range(6):
+        s.integrate(0.005)
+        o.step(0.005)
+    p, v, _ = s.get_state()
+    assert np.abs(v - o.vel).max() < 1e-7
+
+
+def test_launch_count_and_graph_reuse(ljgb_mod):
+    s = ljgb_mod.System(n=1000, density=0.8, temperature=1.0, canonical=1)
+    c0 = s.launch_count()
+    s.integrate(0.005, 10)
+    s.sync()
+    # TVN periodic: drift, pairs, reduce, tvn_finish, observables per step
+    assert s.launch_count() - c0 == 50

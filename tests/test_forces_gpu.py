@@ -1,0 +1,160 @@
+"""Force / energy / virial parity of the CUDA pair kernels (GPU tests).
+
+Every case goes through the C ABI (ljgb -> liblj_gb300.so) and is compared
+with the FP64 oracle restatement on identical seeded inputs.  Gate of the
+mixed-precision path (written here, stated in the spec terms):
+per-particle force error |dF_i| / rms|F| <= 1e-5 for every particle and the
+99th percentile of |dF_i| / |F_i| <= 1e-5; V and the virial within 1e-6
+relative.  The FP64 path must agree to 1e-11.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import lj_testutil as U
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+MIXED_RMS_TOL = 1e-5
+MIXED_P99_TOL = 1e-5
+ENERGY_TOL = 1e-6
+FP64_TOL = 1e-11
+
+
+def make(ljgb, N, rho, T0=1.0, bc=0, prec=0, eps=1.0, sigma=1.0, canonical=0, shape=None):
+    s = ljgb.System(n=N, density=rho, temperature=T0, boundary=bc, precision=prec, epsilon=eps,
+                    sigma=sigma, canonical=canonical)
+    if shape is not None:
+        s.set_kernel_shape(shape)
+    return s
+
+
+def check_against_oracle(oracle_mod, s, pos, L, periodic, prec, eps=1.0, sigma=1.0, rows=None):
+    pos_d, _, F = s.get_state()
+    e, w = s.pair_sums()
+    obs = s.observables()
+    r = oracle_mod.f64_forces(pos_d, L, periodic, eps, sigma, rows=rows)
+    i0, i1 = (0, s.n) if rows is None else rows
+    err = U.force_errors(F[i0:i1], r["F"])
+    if prec == 0:
+        assert err["rms_max"] <= MIXED_RMS_TOL, err
+        assert err["rel_p99"] <= MIXED_P99_TOL, err
+        etol = ENERGY_TOL
+    else:
+        assert err["rms_max"] <= FP64_TOL, err
+        etol = FP64_TOL
+    scale_e = np.abs(r["e"]).max()
+    assert np.abs(e[i0:i1] - r["e"]).max() <= etol * scale_e * 10
+    if rows is None:
+        assert obs["V"] == pytest.approx(r["V"], rel=etol, abs=etol * abs(r["V"]) + 1e-9)
+        assert obs["W"] == pytest.approx(r["W"], rel=etol, abs=etol * abs(r["W"]) + 1e-9)
+    return err
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["mixed", "fp64"])
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_golden_states(ljgb_mod, oracle_mod, path, prec):
+    g = dict(np.load(path))
+    N, rho, bc = int(g["N"]), float(g["rho"]), int(g["bc"])
+    s = make(ljgb_mod, N, rho, float(g["T0"]), bc, prec)
+    pos = g["pos0"][:, :3].astype(np.float64)
+    s.set_state(pos, g["vel0"][:, :3].astype(np.float64))
+    s.calculate_forces()
+    check_against_oracle(oracle_mod, s, pos, s.L, bc == 0, prec)
+    # the reference's own float path agrees within its float storage
+    _, _, F = s.get_state()
+    Fref = g["frc0"][:, :3].astype(np.float64)
+    rms = np.sqrt(np.mean(np.sum(Fref ** 2, 1)))
+    assert (np.linalg.norm(F - Fref, axis=1) / rms).max() < 2e-4
+    obs = s.observables()
+    T_ref, K_ref, V_ref, P_ref, U_ref = g["scalars0"][[1, 2, 3, 4, 0]]
+    assert obs["K"] == pytest.approx(K_ref, rel=1e-6)
+    assert obs["T"] == pytest.approx(T_ref, rel=1e-6)
+    assert obs["V"] == pytest.approx(V_ref, rel=1e-5, abs=1e-5)
+    assert obs["P"] == pytest.approx(P_ref, rel=1e-5, abs=1e-5)
+    assert obs["U"] == pytest.approx(U_ref, rel=1e-5, abs=1e-4)
+    s.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["mixed", "fp64"])
+@pytest.mark.parametrize("N,rho", [(2048, 0.85), (4000, 0.85), (1000, 1.1), (3000, 0.3)])
+def test_dense_liquid(ljgb_mod, oracle_mod, N, rho, prec):
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.02, seed=N)
+    s = make(ljgb_mod, N, rho, 1.0, 0, prec)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    check_against_oracle(oracle_mod, s, pos, L, True, prec)
+
+
+@pytest.mark.parametrize("N", [2, 3, 5, 37, 127, 129, 255, 257, 513, 1000])
+def test_ragged_sizes(ljgb_mod, oracle_mod, N):
+    rho = 0.5 if N > 10 else 0.05
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "sc", 0.05, seed=N)
+    s = make(ljgb_mod, N, rho)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    check_against_oracle(oracle_mod, s, pos, L, True, 0)
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2, 3])
+def test_every_kernel_shape(ljgb_mod, oracle_mod, shape):
+    N, rho = 3001, 0.85
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.02, seed=9)
+    s = make(ljgb_mod, N, rho, shape=shape)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    assert s.tune_info()["active"] == shape
+    check_against_oracle(oracle_mod, s, pos, L, True, 0)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["mixed", "fp64"])
+def test_epsilon_sigma(ljgb_mod, oracle_mod, prec):
+    N, rho_red, sigma, eps = 1500, 0.8, 1.3, 0.7
+    # density in sigma units -> particles per volume in length units
+    rho = rho_red / sigma ** 3
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.02 * sigma, seed=4)
+    s = make(ljgb_mod, N, rho, 1.0, 0, prec, eps, sigma)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    check_against_oracle(oracle_mod, s, pos, L, True, prec, eps, sigma)
+
+
+@pytest.mark.parametrize("bc", [1, 2], ids=["wall", "open"])
+def test_non_periodic(ljgb_mod, oracle_mod, bc):
+    N, rho = 1200, 0.6
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "sc", 0.05, seed=5)
+    pos[:7] += [0.3, -0.2, 0.1]   # a few particles just outside the walls
+    s = make(ljgb_mod, N, rho, 1.0, bc, 0)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    check_against_oracle(oracle_mod, s, pos, L, False, 0)
+
+
+def test_large_box_subset(ljgb_mod, oracle_mod):
+    """N = 16384 dense liquid (the benchmark box): 512 seeded rows vs FP64."""
+    N, rho = 16384, 0.85
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.02, seed=2)
+    s = make(ljgb_mod, N, rho)
+    s.set_state(pos, vel)
+    s.calculate_forces()
+    err = check_against_oracle(oracle_mod, s, pos, L, True, 0, rows=(5000, 5512))
+    print("N=16384 force error", err)
+    # net force vanishes (Newton's third law holds pair by pair in the oracle)
+    _, _, F = s.get_state()
+    assert np.abs(F.sum(0)).max() < 1e-6 * np.sqrt(N) * np.sqrt(np.mean(np.sum(F * F, 1)))
+
+
+def test_fp64_and_mixed_agree_on_observables(ljgb_mod):
+    N, rho = 2048, 0.85
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.02, seed=8)
+    out = []
+    for prec in (0, 1):
+        s = make(ljgb_mod, N, rho, 1.0, 0, prec)
+        s.set_state(pos, vel)
+        s.calculate_forces()
+        out.append(s.observables())
+    for k in ("K", "V", "W", "P", "U"):
+        assert out[0][k] == pytest.approx(out[1][k], rel=1e-6), k
