@@ -31,6 +31,8 @@ namespace ljgb {
 
 namespace {
 
+constexpr int kChunk = 16;  // pairs per compensated force partial sum
+
 // One pair in the MIXED path.  d = qi - qj wraps to the minimum image.
 // s = (s/r)^8 [12 (s/r)^6 - 6] (sigma units), a += (s/r)^12, b += (s/r)^6.
 template <bool MASKED>
@@ -135,17 +137,31 @@ __global__ void __launch_bounds__(THREADS) k_pairs_mixed(PairArgs a) {
       const int4* st = sq + s * TILE;
       const bool masked = (cnt < TILE) || (j0 < bi.i0 + bi.n_i && j0 + cnt > bi.i0);
       if (FORCES) {
-        float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
+        // Force sums are folded into the TwoSum accumulators every kChunk
+        // pairs, so a large near-neighbour term rounds at most kChunk-1 later
+        // additions; the energy sums are folded once per tile.
+        float pa = 0.f, pb = 0.f;
         if (!masked) {
-#pragma unroll 8
-          for (int jj = 0; jj < TILE; ++jj) pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb);
+#pragma unroll 1
+          for (int c0 = 0; c0 < TILE; c0 += kChunk) {
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+            for (int jj = c0; jj < c0 + kChunk; ++jj) pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb);
+            two_sum_add(acc[0], fx);
+            two_sum_add(acc[1], fy);
+            two_sum_add(acc[2], fz);
+          }
         } else {
-          for (int jj = 0; jj < cnt; ++jj)
-            pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb);
+          for (int c0 = 0; c0 < cnt; c0 += kChunk) {
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+            const int c1 = min(cnt, c0 + kChunk);
+            for (int jj = c0; jj < c1; ++jj)
+              pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb);
+            two_sum_add(acc[0], fx);
+            two_sum_add(acc[1], fy);
+            two_sum_add(acc[2], fz);
+          }
         }
-        two_sum_add(acc[0], fx);
-        two_sum_add(acc[1], fy);
-        two_sum_add(acc[2], fz);
         two_sum_add(acc[3], pa);
         two_sum_add(acc[4], pb);
       }
@@ -270,10 +286,10 @@ __global__ void __launch_bounds__(THREADS) k_pairs_fp64(PairArgs a) {
       for (int jj = 0; jj < cnt; ++jj) {
         const double4_32a xj = st[jj];
         double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        if (periodic) {
-          dx = fma(-box.L, rint(dx * box.invL), dx);
-          dy = fma(-box.L, rint(dy * box.invL), dy);
-          dz = fma(-box.L, rint(dz * box.invL), dz);
+        if (periodic) {  // nearest image, ties away from zero (fast_round, MDSystem.cpp:732-739)
+          dx = fma(-box.L, round(dx * box.invL), dx);
+          dy = fma(-box.L, round(dy * box.invL), dy);
+          dz = fma(-box.L, round(dz * box.invL), dz);
         }
         const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
         double ri = s2 / r2;

@@ -468,14 +468,13 @@ void f64_step(f64_state* s, double dt) {
 /* Part 3: emulation of the device's integer decisions (exact histograms).   */
 /* ------------------------------------------------------------------------ */
 
-/* Device shadow: a periodic coordinate as a 32-bit fraction of the box,
- * q = round(frac(x/L) * 2^32) mod 2^32.  The device computes exactly this in
- * FP64 (floor, multiply by 2^32, round-to-nearest-even via rint, wrap). */
+/* Device shadow: a periodic coordinate as a 32-bit fraction of the box on a
+ * grid of 3 units, q = 3 * rint(frac(x/L) * 2^32 / 3) (<= 2^32 - 1).  The
+ * device computes exactly this in FP64 (floor, scale, round-to-nearest-even). */
 uint32_t emu_fixed_coord(double x, double invL) {
   double f = x * invL;
   f = f - floor(f);
-  double q = rint(f * 4294967296.0);
-  if (q >= 4294967296.0) q -= 4294967296.0;
+  double q = 3.0 * rint(f * (4294967296.0 / 3.0));
   return (uint32_t)q;
 }
 

