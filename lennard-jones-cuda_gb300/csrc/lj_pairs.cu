@@ -139,31 +139,37 @@ __global__ void __launch_bounds__(THREADS) k_pairs_mixed(PairArgs a) {
       if (FORCES) {
         // Force sums are folded into the TwoSum accumulators every kChunk
         // pairs, so a large near-neighbour term rounds at most kChunk-1 later
-        // additions; the energy sums are folded once per tile.
-        float pa = 0.f, pb = 0.f;
+        // additions.  Energy sums go chunk -> tile (plain FP32) -> TwoSum: a
+        // chunk partial is never small next to the tile sum, so the far-field
+        // (s/r)^6 tail is not truncated.
+        float ta = 0.f, tb = 0.f;
         if (!masked) {
 #pragma unroll 1
           for (int c0 = 0; c0 < TILE; c0 += kChunk) {
-            float fx = 0.f, fy = 0.f, fz = 0.f;
+            float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
 #pragma unroll
             for (int jj = c0; jj < c0 + kChunk; ++jj) pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb);
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);
+            ta += pa;
+            tb += pb;
           }
         } else {
           for (int c0 = 0; c0 < cnt; c0 += kChunk) {
-            float fx = 0.f, fy = 0.f, fz = 0.f;
+            float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
             const int c1 = min(cnt, c0 + kChunk);
             for (int jj = c0; jj < c1; ++jj)
               pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb);
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);
+            ta += pa;
+            tb += pb;
           }
         }
-        two_sum_add(acc[3], pa);
-        two_sum_add(acc[4], pb);
+        two_sum_add(acc[3], ta);
+        two_sum_add(acc[4], tb);
       }
       if (HIST && valid_i) {
         for (int jj = 0; jj < cnt; ++jj) {

@@ -49,6 +49,7 @@ struct DevBuf {
 };
 
 struct GraphEntry {
+  cudaGraph_t graph = nullptr;  // kept: exec-graph node updates name nodes of this graph
   cudaGraphExec_t exec = nullptr;
   int kernels = 0;
   bool profiled = false;
@@ -173,8 +174,10 @@ PairArgs pair_args(lj_system* s) {
 int nblocks(const lj_system* s) { return (int)s->sched.blocks.size(); }
 
 void clear_graphs(lj_system* s) {
-  for (auto& kv : s->graphs)
+  for (auto& kv : s->graphs) {
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
   s->graphs.clear();
   for (auto e : s->graph_events) cudaEventDestroy(e);
   s->graph_events.clear();
@@ -385,7 +388,7 @@ lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
     }
   }
   LJ_CUDA(s, cudaGraphInstantiate(&ge.exec, g, 0));
-  cudaGraphDestroy(g);
+  ge.graph = g;
   // The capture-time events stay alive with the graph; before every launch
   // the nodes are pointed at fresh events from the pool.
   for (auto& e : ev)

@@ -1,0 +1,53 @@
+"""Command-line driver: one box, n steps, printed observables.
+
+    python lennard-jones-cuda_gb300/ljgb/run_case.py --n 16384 --rho 0.85 --T 1.0 \\
+        --tvn --fcc --jitter 0.02 --steps 10
+
+The counterpart of the reference's task drivers (src/tasks/*) for quick runs
+and for profiling a fixed workload (every step is one CUDA-graph launch of
+the drift / pair / reduce / thermostat / observable kernels).
+"""
+import argparse
+import os
+import sys
+import time
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+import ljgb  # noqa: E402
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--rho", type=float, default=0.85)
+    ap.add_argument("--T", type=float, default=1.0)
+    ap.add_argument("--dt", type=float, default=0.005)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--tvn", action="store_true")
+    ap.add_argument("--fcc", action="store_true")
+    ap.add_argument("--jitter", type=float, default=0.02)
+    ap.add_argument("--bc", type=int, default=0)
+    ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--shape", type=int, default=-1, help="pair-kernel shape (-1: autotune)")
+    a = ap.parse_args(argv)
+    s = ljgb.System(n=a.n, density=a.rho, temperature=a.T, canonical=int(a.tvn), boundary=a.bc,
+                    lattice=ljgb.LATTICE_FCC if a.fcc else ljgb.LATTICE_SC, jitter=a.jitter, seed=a.seed,
+                    precision=ljgb.PREC_FP64 if a.fp64 else ljgb.PREC_MIXED)
+    if not a.fp64:
+        if a.shape >= 0:
+            s.set_kernel_shape(a.shape)
+        else:
+            s.autotune()
+    t0 = time.perf_counter()
+    s.integrate(a.dt, a.steps)
+    o = s.observables()
+    el = time.perf_counter() - t0
+    print("n=%d steps=%d t=%.4f U/N=%.8f T=%.6f P=%.6f wall=%.3fs shape=%s" % (
+        a.n, a.steps, o["t"], o["U"] / a.n, o["T"], o["P"], el, s.tune_info()["active"]))
+    s.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -36,5 +36,7 @@ def force_errors(F, Fref):
     rms = np.sqrt(np.mean(mag ** 2))
     rel = d / np.maximum(mag, 1e-300)
     relrms = d / rms
+    mixed = d / np.maximum(mag, rms)
     return dict(rel_median=float(np.median(rel)), rel_p99=float(np.percentile(rel, 99)),
-                rel_max=float(rel.max()), rms_max=float(relrms.max()), rms_median=float(np.median(relrms)))
+                rel_max=float(rel.max()), rms_max=float(relrms.max()), rms_median=float(np.median(relrms)),
+                gate_max=float(mixed.max()))
