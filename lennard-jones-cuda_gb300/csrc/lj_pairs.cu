@@ -33,6 +33,12 @@ namespace {
 
 constexpr int kChunk = 16;  // pairs per compensated force partial sum
 
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // One pair in the MIXED path.  d = qi - qj wraps to the minimum image.
 // s = (s/r)^8 [12 (s/r)^6 - 6] (sigma units), a += (s/r)^12, b += (s/r)^6.
 template <bool MASKED>
@@ -43,7 +49,9 @@ __device__ __forceinline__ void pair_mixed(const int4 qi, const int4 qj, float k
   const float dy = __int2float_rn((int)((unsigned)qi.y - (unsigned)qj.y));
   const float dz = __int2float_rn((int)((unsigned)qi.z - (unsigned)qj.z));
   const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-  float ri = __fdividef(k2inv, r2);
+  // r2 is in fixed-point units^2, between ~1e14 and ~1.4e19: far from the
+  // subnormal and 2^126 ranges, so the raw approximate reciprocal applies.
+  float ri = k2inv * rcp_approx(r2);
   if (MASKED) ri = excl ? 0.0f : ri;
   const float r6 = ri * ri * ri;
   const float t = __fmaf_rn(12.0f, r6, -6.0f);
@@ -78,8 +86,8 @@ __device__ __forceinline__ int pair_bin(const int4 qi, const int4 qj, float k2, 
 // MIXED-precision persistent pair kernel.
 // THREADS threads, one i-particle each; TILE j-records per stage.
 // ---------------------------------------------------------------------------
-template <int THREADS, int TILE, int STAGES, bool FORCES, bool HIST>
-__global__ void __launch_bounds__(THREADS) k_pairs_mixed(PairArgs a) {
+template <int THREADS, int TILE, int STAGES, int MINB, bool FORCES, bool HIST>
+__global__ void __launch_bounds__(THREADS, MINB) k_pairs_mixed(PairArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   int4* sq = reinterpret_cast<int4*>(smem_raw);
   unsigned* shist = reinterpret_cast<unsigned*>(smem_raw + sizeof(int4) * STAGES * TILE);
@@ -361,18 +369,18 @@ __global__ void __launch_bounds__(THREADS) k_pairs_fp64(PairArgs a) {
 // ---------------------------------------------------------------------------
 namespace {
 
-template <int THREADS, int TILE, int STAGES, bool FORCES, bool HIST>
+template <int THREADS, int TILE, int STAGES, int MINB, bool FORCES, bool HIST>
 cudaError_t launch_mixed_t(const PairArgs& a, int grid, cudaStream_t st) {
   // <= 48 KB: 16 B x STAGES x TILE staging (+ 16 KB histogram), no opt-in needed.
   const size_t smem = sizeof(int4) * STAGES * TILE + (HIST ? sizeof(unsigned) * kMaxHistBins : 0);
-  k_pairs_mixed<THREADS, TILE, STAGES, FORCES, HIST><<<grid, THREADS, smem, st>>>(a);
+  k_pairs_mixed<THREADS, TILE, STAGES, MINB, FORCES, HIST><<<grid, THREADS, smem, st>>>(a);
   return cudaGetLastError();
 }
 
-template <int THREADS, int TILE, int STAGES>
+template <int THREADS, int TILE, int STAGES, int MINB>
 cudaError_t occupancy_mixed_t(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      blocks_per_sm, k_pairs_mixed<THREADS, TILE, STAGES, true, false>, THREADS,
+      blocks_per_sm, k_pairs_mixed<THREADS, TILE, STAGES, MINB, true, false>, THREADS,
       sizeof(int4) * STAGES * TILE);
 }
 
@@ -391,12 +399,20 @@ cudaError_t occupancy_fp64_t(int* blocks_per_sm) {
 
 }  // namespace
 
-// Kernel shapes the autotuner chooses among (threads = i-block size).
+// Kernel shapes the autotuner chooses among (threads = i-block size; MINB =
+// resident CTAs per SM the register allocation must allow).
+#define LJ_SHAPES(X)   \
+  X(0, 128, 256, 3, 8)  \
+  X(1, 64, 256, 3, 16)  \
+  X(2, 256, 256, 3, 4)  \
+  X(3, 128, 512, 2, 8)  \
+  X(4, 128, 256, 3, 10) \
+  X(5, 256, 256, 3, 5)
+
 const PairShape kShapes[] = {
-    {128, 256, 3},
-    {64, 256, 3},
-    {256, 256, 3},
-    {128, 512, 2},
+#define LJ_SHAPE_ROW(i, T, TL, S, M) {T, TL, S},
+    LJ_SHAPES(LJ_SHAPE_ROW)
+#undef LJ_SHAPE_ROW
 };
 const int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
@@ -410,10 +426,11 @@ int fp64_tile() { return kFp64Tile; }
 cudaError_t pair_occupancy(int prec, int shape, int* blocks_per_sm) {
   if (prec == 1) return occupancy_fp64_t<kFp64Threads, kFp64Tile, kFp64Stages>(blocks_per_sm);
   switch (shape) {
-    case 0: return occupancy_mixed_t<128, 256, 3>(blocks_per_sm);
-    case 1: return occupancy_mixed_t<64, 256, 3>(blocks_per_sm);
-    case 2: return occupancy_mixed_t<256, 256, 3>(blocks_per_sm);
-    case 3: return occupancy_mixed_t<128, 512, 2>(blocks_per_sm);
+#define LJ_OCC_CASE(i, T, TL, S, M) \
+  case i:                           \
+    return occupancy_mixed_t<T, TL, S, M>(blocks_per_sm);
+    LJ_SHAPES(LJ_OCC_CASE)
+#undef LJ_OCC_CASE
   }
   return cudaErrorInvalidValue;
 }
@@ -421,17 +438,15 @@ cudaError_t pair_occupancy(int prec, int shape, int* blocks_per_sm) {
 cudaError_t launch_pairs(int prec, int shape, bool forces, bool hist, const PairArgs& a, int grid,
                          cudaStream_t st) {
   if (prec == 1) return launch_fp64_t<kFp64Threads, kFp64Tile, kFp64Stages>(a, grid, st);
-#define LJ_DISPATCH(T, TL, S)                                                     \
-  if (forces && !hist) return launch_mixed_t<T, TL, S, true, false>(a, grid, st); \
-  if (forces && hist) return launch_mixed_t<T, TL, S, true, true>(a, grid, st);   \
-  return launch_mixed_t<T, TL, S, false, true>(a, grid, st);
   switch (shape) {
-    case 0: { LJ_DISPATCH(128, 256, 3) }
-    case 1: { LJ_DISPATCH(64, 256, 3) }
-    case 2: { LJ_DISPATCH(256, 256, 3) }
-    case 3: { LJ_DISPATCH(128, 512, 2) }
+#define LJ_LAUNCH_CASE(i, T, TL, S, M)                                                  \
+  case i:                                                                               \
+    if (forces && !hist) return launch_mixed_t<T, TL, S, M, true, false>(a, grid, st); \
+    if (forces && hist) return launch_mixed_t<T, TL, S, M, true, true>(a, grid, st);   \
+    return launch_mixed_t<T, TL, S, M, false, true>(a, grid, st);
+    LJ_SHAPES(LJ_LAUNCH_CASE)
+#undef LJ_LAUNCH_CASE
   }
-#undef LJ_DISPATCH
   return cudaErrorInvalidValue;
 }
 

@@ -31,10 +31,24 @@ def main(argv=None):
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--shape", type=int, default=-1, help="pair-kernel shape (-1: autotune)")
+    ap.add_argument("--time-shapes", action="store_true", help="print the pair-kernel time of every shape")
     a = ap.parse_args(argv)
     s = ljgb.System(n=a.n, density=a.rho, temperature=a.T, canonical=int(a.tvn), boundary=a.bc,
                     lattice=ljgb.LATTICE_FCC if a.fcc else ljgb.LATTICE_SC, jitter=a.jitter, seed=a.seed,
                     precision=ljgb.PREC_FP64 if a.fp64 else ljgb.PREC_MIXED)
+    if a.time_shapes and not a.fp64:
+        info = s.tune_info()
+        for k, sh in enumerate(info["shapes"]):
+            s.set_kernel_shape(k)
+            s.integrate(a.dt, 3)
+            s.profile(True)
+            s.integrate(a.dt, a.steps)
+            p = s.profile_read()
+            s.profile(False)
+            pairs = a.n * (a.n - 1)
+            ms = p["pair_ms"] / max(1, p["pair_launches"])
+            print("shape %d %s: pair kernel %.4f ms (%.3e pairs/s), step %.4f ms" % (
+                k, sh, ms, pairs / (ms * 1e-3), p["step_ms"] / max(1, p["steps"])))
     if not a.fp64:
         if a.shape >= 0:
             s.set_kernel_shape(a.shape)

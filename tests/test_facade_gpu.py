@@ -30,17 +30,19 @@ def test_driver_runs(ljlib, tmp_path):
     exe = build_driver(ljlib, tmp_path)
     out = subprocess.run([exe, "200"], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
-    txt = out.stdout
-    num = lambda key: float(re.search(key + r"=([-0-9.eE+]+)", txt).group(1))
-    assert num("init T") == pytest.approx(1.312, rel=1e-9)     # exact-T0 initial state
-    assert num("L") == pytest.approx((512 / 0.316) ** (1 / 3), rel=1e-12)
-    assert num("tvn T") == pytest.approx(1.312, rel=0.02)       # TVN holds T near T0
-    assert int(re.search(r"tvn .*av_iters=(\d+)", txt).group(1)) == 200
-    assert int(re.search(r"evn .*av_iters=(\d+)", txt).group(1)) == 200
-    assert abs(num("<T>") - 1.312) < 0.2
-    assert int(num("total")) == 512 * 511                     # every ordered pair binned (clamp rule)
-    peak = num("peak_r")
-    assert 1.0 < peak < 1.3                                     # first shell of the LJ fluid
-    assert num("norm") == pytest.approx(1.0, abs=0.02)         # velocity density integrates to ~1
-    assert num("multi t") == pytest.approx(0.005 * 450, rel=1e-9)
-    assert int(re.search(r"multi .*av_iters=(\d+)", txt).group(1)) == 250
+    lines = {}
+    for line in out.stdout.splitlines():
+        head, *kv = line.split()
+        lines[head] = dict(x.split("=", 1) for x in kv if "=" in x)
+    init, tvn, evn, rdf, velo, multi = (lines[k] for k in ("init", "tvn", "evn", "rdf", "velo", "multi"))
+    assert float(init["T"]) == pytest.approx(1.312, rel=1e-9)          # exact-T0 initial state
+    assert float(init["L"]) == pytest.approx((512 / 0.316) ** (1 / 3), rel=1e-12)
+    assert float(tvn["T"]) == pytest.approx(1.312, rel=0.02)          # TVN holds T near T0
+    assert int(tvn["av_iters"]) == 200
+    assert int(evn["av_iters"]) == 200
+    assert abs(float(evn["<T>"]) - 1.312) < 0.2
+    assert int(rdf["total"]) == 512 * 511                             # every ordered pair binned (clamp rule)
+    assert 1.0 < float(rdf["peak_r"]) < 1.3                            # first shell of the LJ fluid
+    assert float(velo["norm"]) == pytest.approx(1.0, abs=0.02)        # velocity density integrates to ~1
+    assert float(multi["t"]) == pytest.approx(0.005 * 450, rel=1e-9)
+    assert int(multi["av_iters"]) == 250
