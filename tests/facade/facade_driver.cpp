@@ -49,11 +49,13 @@ int main(int argc, char** argv) {
               syst.av_U_tot / syst.av_iters / config.N, syst.av_p_tot / syst.av_iters, syst.av_T_tot / syst.av_iters,
               syst.av_iters, nsum / steps);
   SplineFunction g = syst.RDF();
+  // The last r^2 bin collects every pair beyond the histogram (the
+  // reference GPU rule, MDSystem.cu:39), so the peak search skips it.
   double gmax = 0, rmax = 0;
-  for (auto& p : g.vals)
-    if (p.second > gmax) {
-      gmax = p.second;
-      rmax = p.first;
+  for (size_t k = 0; k + 1 < g.vals.size(); ++k)
+    if (g.vals[k].second > gmax) {
+      gmax = g.vals[k].second;
+      rmax = g.vals[k].first;
     }
   long long total = 0;
   for (int c : syst.NdNdr2) total += c;
