@@ -246,6 +246,24 @@ lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_
                            int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin,
                            int32_t* block_info, int32_t max_blocks);
 
+/* All-pairs LJ forces for callers that cannot allocate device memory (code
+ * running inside another framework's memory pool or a stream capture, loops
+ * that must not allocate after start-up, embedders whose allocator owns the
+ * GPU).  No counterpart in the reference.  pos4: device float4[n] positions
+ * (w ignored); force4: device float4[n] out, xyz = force (eps = sigma = 1),
+ * w = sum_j (r^-12 - r^-6), as calculateNForces writes Force; sums (host,
+ * may be NULL): {V, W} with V = 4 sum_{i<j}[r^-12 - r^-6] and W = sum over
+ * ordered pairs of r.f.  Minimum image when periodic != 0 (box side `box`).
+ * Enqueued on `stream` (NULL: default stream) and synchronised before
+ * returning.  Allocates nothing: every intermediate lives in one fixed
+ * __device__ array (about 4.4 MB per GPU, held from library load to process
+ * exit), so n is limited to 16384 (larger n: LJ_ERR_INVALID).  All calls on
+ * a device share that array and it keeps the last call's contents: calls
+ * whose GPU work overlaps race.  The first call on a device looks up the
+ * array's address; make it before any stream capture. */
+lj_status lj_forces_static(const float* pos4, float* force4, double* sums, int32_t n, float box,
+                           int32_t periodic, void* stream);
+
 /* Page-locked host memory for lj_set_state / lj_get_state buffers: copies
  * from and to it run as direct DMA.  NULL on failure; free with lj_host_free. */
 void* lj_host_alloc(size_t bytes);

@@ -25,6 +25,7 @@ SOURCES = [
     "lj_pairs.cu",
     "lj_integrate.cu",
     "lj_compat.cu",
+    "lj_noalloc.cu",
     "lj_system.cpp",
     "lj_schedule.cpp",
     "lj_init.cpp",
