@@ -15,6 +15,7 @@
 
 #include "lj_device.cuh"
 #include "lj_kernels.h"
+#include "lj_stepdev.cuh"
 
 namespace ljgb {
 
@@ -31,23 +32,6 @@ __device__ __forceinline__ void store_shadow(const StateArgs& s, const DevScalar
   q.w = 0;
   s.q[p] = q;
   s.xd[p] = make_double4_32a(x, y, z, 0.0);
-}
-
-// ApplyBoundaryConditions for one particle (MDSystem.cpp:406-436).
-__device__ __forceinline__ void apply_bc(int bc, double L, double (&x)[3], double (&v)[3]) {
-  if (bc == 0) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (x[c] < 0.) x[c] += L;
-      if (x[c] > L) x[c] -= L;
-    }
-  } else if (bc == 1) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (x[c] < 0. && v[c] < 0) v[c] = -v[c];
-      if (x[c] > L && v[c] > 0) v[c] = -v[c];
-    }
-  }
 }
 
 // Block-wide min/max of the positions (for the fixed-point frame of walls /
@@ -86,15 +70,6 @@ __device__ __forceinline__ void block_bbox(const StateArgs& s, int B, bool valid
       s.blk_part[(size_t)B * 8 + 3 + c] = b;
     }
   }
-}
-
-// Sum of blk_part[b][slot] over the blocks of one box, fixed order, valid in
-// thread 0 (every CTA that calls this obtains the same bits).
-__device__ __forceinline__ double box_sum(const StateArgs& s, int b0, int b1, int slot, double* sh) {
-  double acc[1] = {0.0};
-  for (int b = b0 + (int)threadIdx.x; b < b1; b += blockDim.x) acc[0] += s.blk_part[(size_t)b * 8 + slot];
-  block_sum<1>(acc, sh);
-  return acc[0];
 }
 
 }  // namespace
@@ -341,56 +316,77 @@ __global__ void k_tvn_finish(StateArgs s) {
   if (tid == 0) s.blk_part[(size_t)B * 8 + 0] = part[0];
 }
 
-// CalculateParameters (MDSystem.cpp:325-359) per box, plus t += dt for steps
-// (MDSystem.cpp:582) and the optional per-step record.
+// CalculateParameters (MDSystem.cpp:325-359) per box (one CTA per box).
 template <int MODE>
 __global__ void k_observables(StateArgs s) {
   __shared__ double sh[32];
-  const int sys = blockIdx.x;
-  const BoxArgs box = s.boxes[sys];
-  const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
-  const double K = box_sum(s, b0, b1, 0, sh);
-  const double V = box_sum(s, b0, b1, 1, sh);
-  const double W = box_sum(s, b0, b1, 2, sh);
-  if (threadIdx.x != 0) return;
-  DevScalars& sc = s.sc[sys];
-  const double N = (double)box.N;
-  const double T = 2. * K / 3. / N;
-  const double P = (W / 6. + N * T) / (N / box.rho);
-  const double U = K + V;
-  sc.K = K;
-  sc.V = V;
-  sc.W = W;
-  sc.T = T;
-  sc.P_press = P;
-  sc.U = U;
-  if (MODE != MODE_TVN) sc.Tkin = 0.0;
-  if (MODE != MODE_FORCES_ONLY) {
-    sc.t += box.dt;
-    sc.step += 1;
+  observables_box<MODE>(s, blockIdx.x, sh);
+}
+
+// Predictor of the fused step: the shadow of x + dt v + dt^2 F / 2 (the
+// positions the next pair kernel evaluates), periodic boxes.
+__global__ void k_predict(StateArgs s) {
+  const BlockInfo bi = s.blocks[blockIdx.x];
+  if ((int)threadIdx.x >= bi.n_i) return;
+  const int p = bi.p0 + bi.i0 + threadIdx.x;
+  const double dt = s.boxes[bi.sys].dt;
+  double xp[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = (size_t)c * s.npad + p;
+    xp[c] = s.x[k] + dt * s.v[k] + dt * dt * s.f[k] / 2.;
   }
-  sc.av_iters += 1;
-  sc.av_U += U;
-  sc.av_p += P;
-  sc.av_T += T;
-  if (!isfinite(K) || !isfinite(V) || !isfinite(W)) atomicOr(s.status, LJ_DEVFLAG_NONFINITE);
-  if (sc.rec_cap > 0 && MODE != MODE_FORCES_ONLY) {
-    DevRecord& r = s.records[(size_t)sys * s.rec_stride + (size_t)(sc.rec_count % sc.rec_cap)];
-    r.t = sc.t;
-    r.K = K;
-    r.V = V;
-    r.T = T;
-    r.P = P;
-    r.U = U;
-    r.W = W;
-    r.Pshear = sc.Pshear;
-    r.Tkin = sc.Tkin;
-    r.av_U = sc.av_U;
-    r.av_T = sc.av_T;
-    r.av_p = sc.av_p;
-    r.av_iters = sc.av_iters;
-    r.step = sc.step;
-    sc.rec_count += 1;
+  s.q[p] = shadow_of(s.sc[bi.sys], xp[0], xp[1], xp[2]);
+}
+
+// Close of a fused TVN step (MDSystem.cpp:498-506 and :578-579): with chi of
+// the box computed by the pair kernel's last block, v = (2 chi - 1) v +
+// chi dt tF, boundaries, K, the next step's predictor, and -- in the last
+// CTA to finish -- the observables of every box.
+__global__ void k_tvn_close(StateArgs s) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  const int B = blockIdx.x;
+  const BlockInfo bi = s.blocks[B];
+  const int tid = threadIdx.x;
+  const BoxArgs box = s.boxes[bi.sys];
+  const DevScalars& sc = s.sc[bi.sys];
+  const double chi = sc.chi;
+  const double dt = box.dt;
+  double part[1] = {0.0};
+  if (tid < bi.n_i) {
+    const int p = bi.p0 + bi.i0 + tid;
+    double x[3], v[3], f[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      v[c] = (2. * chi - 1.) * s.v[k] + chi * dt * s.tf[k];
+      x[c] = s.x[k];
+      f[c] = s.f[k];
+    }
+    apply_bc(box.bc, box.L, x, v);
+    double xp[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      s.v[k] = v[c];
+      s.x[k] = x[c];
+      xp[c] = x[c] + dt * v[c] + dt * dt * f[c] / 2.;
+    }
+    s.q_next[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
+    part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  }
+  block_sum<1>(part, sh);
+  if (tid == 0) {
+    s.blk_part[(size_t)B * 8 + 0] = part[0];
+    __threadfence();
+    last = (atomicAdd(s.glob_cnt + 1, 1) == s.nblocks - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int sys = 0; sys < s.nsys; ++sys) observables_box<MODE_TVN>(s, sys, sh);
+    if (tid == 0) s.glob_cnt[1] = 0;
   }
 }
 
@@ -510,6 +506,16 @@ cudaError_t launch_observables(const StateArgs& s, int nsys, int mode, cudaStrea
   if (mode == MODE_FORCES_ONLY) k_observables<MODE_FORCES_ONLY><<<nsys, kObsThreads, 0, st>>>(s);
   else if (mode == MODE_EVN) k_observables<MODE_EVN><<<nsys, kObsThreads, 0, st>>>(s);
   else k_observables<MODE_TVN><<<nsys, kObsThreads, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t st) {
+  k_predict<<<nblocks, bi, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tvn_close(const StateArgs& s, int nblocks, int bi, cudaStream_t st) {
+  k_tvn_close<<<nblocks, bi, 0, st>>>(s);
   return cudaGetLastError();
 }
 

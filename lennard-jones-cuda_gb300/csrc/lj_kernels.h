@@ -37,6 +37,7 @@ struct PairArgs {
   HistArgs hist;
 };
 
+
 struct PairShape {
   int threads;  // CTA size = i-block length (one i per thread)
   int tile;     // j records per staged tile
@@ -51,6 +52,8 @@ int fp64_tile();
 cudaError_t pair_occupancy(int prec, int shape, int* blocks_per_sm);
 cudaError_t launch_pairs(int prec, int shape, bool forces, bool hist, const PairArgs& a, int grid,
                          cudaStream_t st);
+struct FusedPairArgs;
+cudaError_t launch_pairs_fused(int shape, int mode, const FusedPairArgs& a, int grid, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Integrator / reduction kernels (lj_integrate.cu).  All operate on the
@@ -77,9 +80,21 @@ struct StateArgs {
   DevRecord* records;          // per box ring (rec_cap entries each)
   int rec_stride;              // ring capacity per box
   int* status;
+  int4* q_next;                // fused step: predictor shadow for the next step
+  int* blk_cnt;                // fused step: segments finished per i-block
+  int* glob_cnt;               // fused step: blocks finished (2 counters)
+  int nblocks;                 // i-blocks of all boxes
+  int nsys;                    // boxes
 };
 
 enum StepMode { MODE_FORCES_ONLY = 0, MODE_EVN = 1, MODE_TVN = 2 };
+
+// The pair kernel with the second half of the Verlet step fused into the
+// last CTA of every i-block (epi = MODE_EVN or MODE_TVN).
+struct FusedPairArgs {
+  PairArgs pair;
+  StateArgs st;
+};
 
 cudaError_t launch_drift_mode(const StateArgs& s, int nblocks, int bi, int mode, cudaStream_t st);
 cudaError_t launch_bbox(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
@@ -90,6 +105,8 @@ cudaError_t launch_tvn_finish(const StateArgs& s, int nblocks, int bi, cudaStrea
 cudaError_t launch_observables(const StateArgs& s, int nsys, int mode, cudaStream_t st);
 cudaError_t launch_velocity_hist(const StateArgs& s, int nblocks, int bi, double step, int nb,
                                  unsigned long long* counts, cudaStream_t st);
+cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
+cudaError_t launch_tvn_close(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,

@@ -26,6 +26,7 @@
 
 #include "lj_device.cuh"
 #include "lj_kernels.h"
+#include "lj_stepdev.cuh"
 
 namespace ljgb {
 
@@ -86,12 +87,18 @@ __device__ __forceinline__ int pair_bin(const int4 qi, const int4 qj, float k2, 
 // MIXED-precision persistent pair kernel.
 // THREADS threads, one i-particle each; TILE j-records per stage.
 // ---------------------------------------------------------------------------
-template <int THREADS, int TILE, int STAGES, int MINB, bool FORCES, bool HIST>
-__global__ void __launch_bounds__(THREADS, MINB) k_pairs_mixed(PairArgs a) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+// EPI = 0: partial segments only.  EPI = MODE_EVN / MODE_TVN: the CTA that
+// writes the last segment of an i-block also runs the second half of the
+// Verlet step for that block (fused_block_step), and the CTA that finishes
+// the last block runs the per-box observables (EVN) or the TVN scale (TVN).
+// Completion is detected with atomic counters only; no CTA waits on another.
+template <int THREADS, int TILE, int STAGES, bool FORCES, bool HIST, int EPI>
+__device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& st, unsigned char* smem_raw) {
   int4* sq = reinterpret_cast<int4*>(smem_raw);
   unsigned* shist = reinterpret_cast<unsigned*>(smem_raw + sizeof(int4) * STAGES * TILE);
   __shared__ uint64_t bars[STAGES];
+  __shared__ double shd[EPI ? 4 * 32 : 1];
+  __shared__ int sflag;
 
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
@@ -212,6 +219,34 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pairs_mixed(PairArgs a) {
       }
 #pragma unroll
       for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
+      if (EPI) {
+        // Last segment of block B?  (fence, then count; the CTA that
+        // completes the count owns the block's epilogue)
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) sflag = (atomicAdd(st.blk_cnt + B, 1) == bi.seg_count - 1);
+        __syncthreads();
+        if (sflag) {
+          __threadfence();
+          fused_block_step<EPI>(st, B, shd);
+          __syncthreads();
+          if (tid == 0) {
+            st.blk_cnt[B] = 0;
+            __threadfence();
+            sflag = (atomicAdd(st.glob_cnt, 1) == st.nblocks - 1);
+          }
+          __syncthreads();
+          if (sflag) {
+            __threadfence();
+            for (int sys = 0; sys < st.nsys; ++sys) {
+              if (EPI == MODE_EVN) observables_box<MODE_EVN>(st, sys, shd);
+              else tvn_chi_box(st, sys, shd);
+            }
+            if (tid == 0) st.glob_cnt[0] = 0;
+          }
+          __syncthreads();
+        }
+      }
       if (block_end && !last) {
         ++B;
         bi = a.blocks[B];
@@ -240,6 +275,18 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pairs_mixed(PairArgs a) {
     for (int b = tid; b < a.hist.nb; b += THREADS)
       if (shist[b]) atomicAdd(a.hist.counts + b, (unsigned long long)shist[b]);
   }
+}
+
+template <int THREADS, int TILE, int STAGES, int MINB, bool FORCES, bool HIST>
+__global__ void __launch_bounds__(THREADS, MINB) k_pairs_mixed(PairArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  pairs_body<THREADS, TILE, STAGES, FORCES, HIST, 0>(a, StateArgs{}, smem_raw);
+}
+
+template <int THREADS, int TILE, int STAGES, int MINB, int EPI>
+__global__ void __launch_bounds__(THREADS, MINB) k_pairs_mixed_fused(FusedPairArgs f) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  pairs_body<THREADS, TILE, STAGES, true, false, EPI>(f.pair, f.st, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -378,6 +425,14 @@ cudaError_t launch_mixed_t(const PairArgs& a, int grid, cudaStream_t st) {
 }
 
 template <int THREADS, int TILE, int STAGES, int MINB>
+cudaError_t launch_fused_t(int mode, const FusedPairArgs& f, int grid, cudaStream_t st) {
+  const size_t smem = sizeof(int4) * STAGES * TILE;
+  if (mode == MODE_EVN) k_pairs_mixed_fused<THREADS, TILE, STAGES, MINB, MODE_EVN><<<grid, THREADS, smem, st>>>(f);
+  else k_pairs_mixed_fused<THREADS, TILE, STAGES, MINB, MODE_TVN><<<grid, THREADS, smem, st>>>(f);
+  return cudaGetLastError();
+}
+
+template <int THREADS, int TILE, int STAGES, int MINB>
 cudaError_t occupancy_mixed_t(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       blocks_per_sm, k_pairs_mixed<THREADS, TILE, STAGES, MINB, true, false>, THREADS,
@@ -446,6 +501,17 @@ cudaError_t launch_pairs(int prec, int shape, bool forces, bool hist, const Pair
     return launch_mixed_t<T, TL, S, M, false, true>(a, grid, st);
     LJ_SHAPES(LJ_LAUNCH_CASE)
 #undef LJ_LAUNCH_CASE
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pairs_fused(int shape, int mode, const FusedPairArgs& f, int grid, cudaStream_t st) {
+  switch (shape) {
+#define LJ_FUSED_CASE(i, T, TL, S, M) \
+  case i:                             \
+    return launch_fused_t<T, TL, S, M>(mode, f, grid, st);
+    LJ_SHAPES(LJ_FUSED_CASE)
+#undef LJ_FUSED_CASE
   }
   return cudaErrorInvalidValue;
 }

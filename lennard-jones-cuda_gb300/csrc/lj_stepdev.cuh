@@ -1,0 +1,194 @@
+// lj_stepdev.cuh -- device pieces of the Verlet step shared by the integrator
+// kernels (lj_integrate.cu) and the fused epilogue of the pair kernel
+// (lj_pairs.cu): boundaries, the fixed-point predictor, per-block segment
+// reduction + kick, and the per-box observables of CalculateParameters.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lj_device.cuh"
+#include "lj_kernels.h"
+
+namespace ljgb {
+
+// ApplyBoundaryConditions for one particle (MDSystem.cpp:406-436).
+__device__ __forceinline__ void apply_bc(int bc, double L, double (&x)[3], double (&v)[3]) {
+  if (bc == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (x[c] < 0.) x[c] += L;
+      if (x[c] > L) x[c] -= L;
+    }
+  } else if (bc == 1) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (x[c] < 0. && v[c] < 0) v[c] = -v[c];
+      if (x[c] > L && v[c] > 0) v[c] = -v[c];
+    }
+  }
+}
+
+__device__ __forceinline__ int4 shadow_of(const DevScalars& sc, double x, double y, double z) {
+  return make_int4(fixed_coord(x, sc.origin[0], sc.invP), fixed_coord(y, sc.origin[1], sc.invP),
+                   fixed_coord(z, sc.origin[2], sc.invP), 0);
+}
+
+// Sum of blk_part[b][slot] over the blocks of one box, fixed order, valid in
+// thread 0 (every CTA that calls this obtains the same bits).
+__device__ __forceinline__ double box_sum(const StateArgs& s, int b0, int b1, int slot, double* sh) {
+  double acc[1] = {0.0};
+  for (int b = b0 + (int)threadIdx.x; b < b1; b += blockDim.x) acc[0] += __ldcg(s.blk_part + (size_t)b * 8 + slot);
+  block_sum<1>(acc, sh);
+  return acc[0];
+}
+
+// CalculateParameters (MDSystem.cpp:325-359) for box `sys`, plus t += dt for
+// steps (MDSystem.cpp:582) and the optional per-step record.  Block-wide call;
+// thread 0 writes.
+template <int MODE>
+__device__ __forceinline__ void observables_box(const StateArgs& s, int sys, double* sh) {
+  const BoxArgs box = s.boxes[sys];
+  const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
+  const double K = box_sum(s, b0, b1, 0, sh);
+  const double V = box_sum(s, b0, b1, 1, sh);
+  const double W = box_sum(s, b0, b1, 2, sh);
+  if (threadIdx.x != 0) return;
+  DevScalars& sc = s.sc[sys];
+  const double N = (double)box.N;
+  const double T = 2. * K / 3. / N;
+  const double P = (W / 6. + N * T) / (N / box.rho);
+  const double U = K + V;
+  sc.K = K;
+  sc.V = V;
+  sc.W = W;
+  sc.T = T;
+  sc.P_press = P;
+  sc.U = U;
+  if (MODE != MODE_TVN) sc.Tkin = 0.0;
+  if (MODE != MODE_FORCES_ONLY) {
+    sc.t += box.dt;
+    sc.step += 1;
+  }
+  sc.av_iters += 1;
+  sc.av_U += U;
+  sc.av_p += P;
+  sc.av_T += T;
+  if (!isfinite(K) || !isfinite(V) || !isfinite(W)) atomicOr(s.status, LJ_DEVFLAG_NONFINITE);
+  if (sc.rec_cap > 0 && MODE != MODE_FORCES_ONLY) {
+    DevRecord& r = s.records[(size_t)sys * s.rec_stride + (size_t)(sc.rec_count % sc.rec_cap)];
+    r.t = sc.t;
+    r.K = K;
+    r.V = V;
+    r.T = T;
+    r.P = P;
+    r.U = U;
+    r.W = W;
+    r.Pshear = sc.Pshear;
+    r.Tkin = sc.Tkin;
+    r.av_U = sc.av_U;
+    r.av_T = sc.av_T;
+    r.av_p = sc.av_p;
+    r.av_iters = sc.av_iters;
+    r.step = sc.step;
+    sc.rec_count += 1;
+  }
+}
+
+// TVN scale of box `sys` (MDSystem.cpp:498-499) from the half-kicked
+// velocities' block sums (slot 3).  Block-wide call; thread 0 writes.
+__device__ __forceinline__ void tvn_chi_box(const StateArgs& s, int sys, double* sh) {
+  const BoxArgs box = s.boxes[sys];
+  const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
+  const double tv2 = box_sum(s, b0, b1, 3, sh);
+  if (threadIdx.x == 0) {
+    const double Tkin = tv2 * (1. / 3. / box.N);
+    s.sc[sys].Tkin = Tkin;
+    s.sc[sys].chi = sqrt(box.T0 / Tkin);
+  }
+}
+
+// Fused second half of a step for block B, run by the CTA that wrote the last
+// pair-kernel segment of the block (blockDim.x = the i-block length).
+// Starts from the state at the beginning of the step (x_n, v_n, F_n); the
+// forces of this step were computed at x_{n+1} = x_n + dt v_n + dt^2 F_n / 2,
+// the predictor written by the previous step, recomputed here bit for bit.
+//   EVN (MDSystem.cpp:443-463): v_{n+1} = v_n + dt F_n/2 + dt F_{n+1}/2,
+//       boundaries, K, and the predictor of the next step into q_next.
+//   TVN (MDSystem.cpp:469-497): tF = F_n/2 + F_{n+1}/2, the half-kicked
+//       velocity's sum of squares (slot 3); v and the boundaries follow in
+//       k_tvn_close once chi is known.
+// Block partials: [0] K (EVN), [1] V, [2] W, [3] sum tv^2 (TVN).
+template <int MODE>
+__device__ __forceinline__ void fused_block_step(const StateArgs& s, int B, double* sh) {
+  const BlockInfo bi = s.blocks[B];
+  const int tid = threadIdx.x;
+  const bool valid = tid < bi.n_i;
+  const int p = bi.p0 + bi.i0 + tid;
+  const BoxArgs box = s.boxes[bi.sys];
+  const DevScalars& sc = s.sc[bi.sys];
+  const double dt = box.dt;
+  double part[4] = {0., 0., 0., 0.};
+  if (valid) {
+    double S[5] = {0., 0., 0., 0., 0.};
+    for (int k = 0; k < bi.seg_count; ++k) {
+      const size_t base = (size_t)(bi.seg_first + k) * 5 * s.bi_threads + tid;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) S[c] += (double)__ldcg(s.partial + base + (size_t)c * s.bi_threads);
+    }
+    const double fs = sc.fscale;
+    const double Fn1[3] = {fs * S[0], fs * S[1], fs * S[2]};
+    const double e = 4.0 * box.eps * (S[3] - S[4]);
+    const double w = 4.0 * box.eps * (12.0 * S[3] - 6.0 * S[4]);
+    s.e[p] = e;
+    s.w[p] = w;
+    part[1] = 0.5 * e;
+    part[2] = w;
+    double x[3], v[3], Fn[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = (size_t)c * s.npad + p;
+      x[c] = s.x[k];
+      v[c] = s.v[k];
+      Fn[c] = s.f[k];
+      x[c] += dt * v[c] + dt * dt * Fn[c] / 2.;
+      s.f[k] = Fn1[c];
+    }
+    if (MODE == MODE_EVN) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        v[c] += dt * Fn[c] / 2.;
+        v[c] += dt * Fn1[c] / 2.;
+      }
+      apply_bc(box.bc, box.L, x, v);
+      double xp[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t k = (size_t)c * s.npad + p;
+        s.x[k] = x[c];
+        s.v[k] = v[c];
+        xp[c] = x[c] + dt * v[c] + dt * dt * Fn1[c] / 2.;
+      }
+      s.q_next[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
+      part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    } else {
+      double tv2 = 0.0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t k = (size_t)c * s.npad + p;
+        s.x[k] = x[c];
+        const double tf = 0.5 * Fn[c] + 0.5 * Fn1[c];
+        s.tf[k] = tf;
+        const double tv = v[c] + dt * tf / 2.;
+        tv2 += tv * tv;
+      }
+      part[3] = tv2;
+    }
+  }
+  block_sum<4>(part, sh);
+  if (tid == 0) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
+  }
+}
+
+}  // namespace ljgb

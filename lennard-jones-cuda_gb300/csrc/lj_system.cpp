@@ -79,8 +79,12 @@ struct lj_system {
 
   // device memory
   DevBuf<double> x, v, f, tf, e, w, stage;
-  DevBuf<int4> q;
+  DevBuf<int4> q, q2;  // fixed-point shadow, double-buffered for the fused step
   DevBuf<double4_32a> xd;
+  DevBuf<int> blk_cnt, glob_cnt;  // fused-step completion counters
+  int qpar = 0;             // which of q / q2 holds the current shadow
+  bool pred_ready = false;  // current shadow = predictor x + dt v + dt^2 F/2 for pred_dt
+  double pred_dt = 0.0;
   DevBuf<BlockInfo> blocks;
   DevBuf<int> cta_tile_begin, cta_block, cta_jt, sys_block_first;
   DevBuf<DevScalars> sc;
@@ -138,7 +142,8 @@ StateArgs state_args(lj_system* s) {
   a.tf = s->tf.p;
   a.e = s->e.p;
   a.w = s->w.p;
-  a.q = s->q.p;
+  a.q = s->qpar ? s->q2.p : s->q.p;
+  a.q_next = s->qpar ? s->q.p : s->q2.p;
   a.xd = s->xd.p;
   a.npad = s->npad;
   a.blocks = s->blocks.p;
@@ -152,12 +157,16 @@ StateArgs state_args(lj_system* s) {
   a.records = s->records.p;
   a.rec_stride = s->rec_cap;
   a.status = s->status.p;
+  a.blk_cnt = s->blk_cnt.p;
+  a.glob_cnt = s->glob_cnt.p;
+  a.nblocks = (int)s->sched.blocks.size();
+  a.nsys = s->nsys;
   return a;
 }
 
 PairArgs pair_args(lj_system* s) {
   PairArgs a{};
-  a.q = s->q.p;
+  a.q = s->qpar ? s->q2.p : s->q.p;
   a.xd = s->xd.p;
   a.blocks = s->blocks.p;
   a.cta_tile_begin = s->cta_tile_begin.p;
@@ -248,6 +257,11 @@ lj_status setup_schedule(lj_system* s) {
   LJ_CUDA(s, s->cta_jt.alloc(s->sched.G));
   LJ_CUDA(s, s->sys_block_first.alloc(s->nsys + 1));
   LJ_CUDA(s, s->blk_part.alloc((size_t)nb * 8));
+  LJ_CUDA(s, s->blk_cnt.alloc(nb));
+  LJ_CUDA(s, s->glob_cnt.alloc(2));
+  LJ_CUDA(s, cudaMemsetAsync(s->blk_cnt.p, 0, sizeof(int) * nb, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * 2, s->stream));
+  s->pred_ready = false;
   // partial: nseg x 5 x BI values of 8 bytes (FP64) or 4 bytes (MIXED)
   const size_t vals = (size_t)s->sched.nseg * 5 * threads;
   LJ_CUDA(s, s->partial.alloc(vals * (s->prec == LJ_PREC_FP64 ? 2 : 1)));
@@ -269,6 +283,7 @@ lj_status setup_schedule(lj_system* s) {
 // ---- kernel sequences ----------------------------------------------------
 
 lj_status enqueue_frame_all(lj_system* s) {
+  s->pred_ready = false;  // the current shadow becomes the positions themselves
   StateArgs a = state_args(s);
   const int nb = nblocks(s);
   LJ_CUDA(s, launch_bbox(a, nb, s->BI, s->stream));
@@ -344,6 +359,34 @@ lj_status enqueue_step(lj_system* s, int mode, cudaEvent_t* ev, bool capture, in
   return LJ_OK;
 }
 
+// Fused step: the pair kernel carries the second half of the Verlet step in
+// the last CTA of each i-block (EVN: everything, one kernel per step; TVN: the
+// chi reduction, then k_tvn_close applies the rescale).  Needs periodic boxes
+// (constant shadow frame) and the MIXED kernel.
+bool use_fused(const lj_system* s) { return s->prec == LJ_PREC_MIXED && !s->any_nonperiodic; }
+
+lj_status enqueue_step_fused(lj_system* s, int mode, cudaEvent_t* ev, bool capture, int* kernels) {
+  StateArgs a = state_args(s);
+  const int nb = nblocks(s);
+  const unsigned flags = capture ? cudaEventRecordExternal : cudaEventRecordDefault;
+  int k = 0;
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[0], s->stream, flags));
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[1], s->stream, flags));
+  FusedPairArgs f{};
+  f.pair = pair_args(s);
+  f.st = a;
+  LJ_CUDA(s, launch_pairs_fused(s->shape, mode, f, s->sched.G, s->stream));
+  ++k;
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[2], s->stream, flags));
+  if (mode == MODE_TVN) {
+    LJ_CUDA(s, launch_tvn_close(a, nb, s->BI, s->stream));
+    ++k;
+  }
+  if (ev) LJ_CUDA(s, cudaEventRecordWithFlags(ev[3], s->stream, flags));
+  if (kernels) *kernels = k;
+  return LJ_OK;
+}
+
 int step_mode(const lj_system* s) {
   // A batch with mixed ensembles steps every box with its own flag inside the
   // kernels; the launch sequence only needs to know whether any box is TVN.
@@ -353,7 +396,9 @@ int step_mode(const lj_system* s) {
 }
 
 lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
-  const int key = mode * 4 + (s->any_nonperiodic ? 2 : 0) + (s->profiling ? 1 : 0);
+  const bool fused = use_fused(s);
+  const int key = mode * 16 + (fused ? 8 : 0) + (fused && s->qpar ? 4 : 0) + (s->any_nonperiodic ? 2 : 0) +
+                  (s->profiling ? 1 : 0);
   auto it = s->graphs.find(key);
   if (it != s->graphs.end()) {
     *out = &it->second;
@@ -368,7 +413,8 @@ lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
     }
   cudaGraph_t g = nullptr;
   LJ_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-  lj_status st = enqueue_step(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels);
+  lj_status st = fused ? enqueue_step_fused(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels)
+                       : enqueue_step(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels);
   cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
   if (st) return st;
   LJ_CUDA(s, ce);
@@ -404,6 +450,10 @@ lj_status check_status(lj_system* s) {
   LJ_CUDA(s, cudaMemcpy(&st, s->status.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (st) {
     LJ_CUDA(s, cudaMemset(s->status.p, 0, sizeof(int)));
+    // A failed launch may leave the fused-step counters mid-count.
+    if (s->blk_cnt.p) LJ_CUDA(s, cudaMemset(s->blk_cnt.p, 0, sizeof(int) * s->blk_cnt.n));
+    if (s->glob_cnt.p) LJ_CUDA(s, cudaMemset(s->glob_cnt.p, 0, sizeof(int) * 2));
+    s->pred_ready = false;
     if (st & LJ_DEVFLAG_TIMEOUT)
       return fail(s, LJ_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the results of that launch are void");
     if (st & LJ_DEVFLAG_NONFINITE)
@@ -423,6 +473,7 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, s->e.alloc(s->npad));
   LJ_CUDA(s, s->w.alloc(s->npad));
   LJ_CUDA(s, s->q.alloc(s->npad));
+  LJ_CUDA(s, s->q2.alloc(s->npad));
   LJ_CUDA(s, s->xd.alloc(s->npad));
   LJ_CUDA(s, s->sc.alloc(s->nsys));
   LJ_CUDA(s, s->dboxes.alloc(s->nsys));
@@ -433,6 +484,7 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, cudaMemsetAsync(s->f.p, 0, sizeof(double) * n3, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->tf.p, 0, sizeof(double) * n3, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->q.p, 0, sizeof(int4) * s->npad, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->q2.p, 0, sizeof(int4) * s->npad, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->xd.p, 0, sizeof(double4_32a) * s->npad, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->sc.p, 0, sizeof(DevScalars) * s->nsys, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->status.p, 0, sizeof(int), s->stream));
@@ -631,7 +683,10 @@ lj_status lj_destroy(lj_system* s) {
   s->w.free();
   s->stage.free();
   s->q.free();
+  s->q2.free();
   s->xd.free();
+  s->blk_cnt.free();
+  s->glob_cnt.free();
   s->blocks.free();
   s->cta_tile_begin.free();
   s->cta_block.free();
@@ -677,6 +732,7 @@ lj_status lj_reinitialize(lj_system* s, const lj_config* cfg) {
 lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
   if (!s) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);
+  s->pred_ready = false;
   if (pos) {
     for (size_t k = 0; k < 3 * (size_t)s->ntotal; ++k)
       if (!std::isfinite(pos[k])) return fail(s, LJ_ERR_INVALID, "position %zu is not finite", k / 3);
@@ -736,10 +792,17 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
     if (st) return st;
   }
   const int mode = step_mode(s);
-  GraphEntry* ge = nullptr;
-  lj_status st = get_graph(s, mode, &ge);
-  if (st) return st;
+  const bool fused = use_fused(s);
+  if (fused && (!s->pred_ready || s->pred_dt != dt)) {
+    LJ_CUDA(s, launch_predict(state_args(s), nblocks(s), s->BI, s->stream));
+    s->launches += 1;
+    s->pred_ready = true;
+    s->pred_dt = dt;
+  }
   for (int k = 0; k < nsteps; ++k) {
+    GraphEntry* ge = nullptr;
+    lj_status st = get_graph(s, mode, &ge);
+    if (st) return st;
     if (ge->profiled) {
       for (int e = 0; e < 4; ++e) {
         cudaEvent_t ev = next_event(s);
@@ -749,6 +812,7 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
     }
     LJ_CUDA(s, cudaGraphLaunch(ge->exec, s->stream));
     s->launches += ge->kernels;
+    if (fused) s->qpar ^= 1;  // the step wrote the next predictor into the other buffer
   }
   return LJ_OK;
 }
@@ -917,6 +981,7 @@ lj_status lj_renormalize_velocities(lj_system* s, int32_t recalc) {
   if (!(Tkin > 0)) return fail(s, LJ_ERR_INVALID, "kinetic temperature is zero; cannot rescale");
   LJ_CUDA(s, launch_scale_velocities(a, nblocks(s), s->BI, 0, std::sqrt(T0 / Tkin), s->stream));
   s->launches += 1;
+  s->pred_ready = false;
   // MDSystem.cpp:386-388: K *= T0/Tkin; T = T0; U = K + V.
   sc[0].K *= T0 / Tkin;
   sc[0].T = T0;
@@ -939,6 +1004,7 @@ lj_status lj_renormalize_velocities_to_energy(lj_system* s, double ust) {
   StateArgs a = state_args(s);
   LJ_CUDA(s, launch_scale_velocities(a, nblocks(s), s->BI, 0, std::sqrt(Kdes / Kold), s->stream));
   s->launches += 1;
+  s->pred_ready = false;
   sc[0].K = Kdes;
   sc[0].U = sc[0].K + sc[0].V;
   return write_scalars(s, sc);

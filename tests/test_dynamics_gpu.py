@@ -169,5 +169,43 @@ def test_launch_count_and_graph_reuse(ljgb_mod):
     c0 = s.launch_count()
     s.integrate(0.005, 10)
     s.sync()
-    # TVN periodic: drift, pairs, reduce, tvn_finish, observables per step
-    assert s.launch_count() - c0 == 50
+    # fused TVN, periodic: one predictor, then pair kernel (+ epilogue) and
+    # k_tvn_close per step
+    assert s.launch_count() - c0 == 1 + 2 * 10
+    c1 = s.launch_count()
+    s.integrate(0.005, 10)
+    assert s.launch_count() - c1 == 2 * 10     # prediction carried over from the last step
+    e = ljgb_mod.System(n=1000, density=0.8, temperature=1.0, canonical=0)
+    c2 = e.launch_count()
+    e.integrate(0.005, 10)
+    assert e.launch_count() - c2 == 1 + 10     # fused EVN: one kernel per step
+    w = ljgb_mod.System(n=1000, density=0.8, temperature=1.0, canonical=0, boundary=1)
+    c3 = w.launch_count()
+    w.integrate(0.005, 10)
+    # walls: drift, frame, quantize, pairs, reduce, observables per step
+    assert w.launch_count() - c3 == 6 * 10
+
+
+def test_fused_matches_unfused_path(ljgb_mod):
+    """The fused step (periodic) and the kernel-per-phase step (taken by
+    FP64 and non-periodic boxes) integrate the same equations: compare the
+    fused mixed path with the FP64 path over 30 steps of both ensembles."""
+    import lj_testutil as U
+    N, rho = 3000, 0.8
+    pos, vel, L = U.lattice_state(N, rho, 1.1, "fcc", 0.02, seed=21)
+    for canonical in (0, 1):
+        out = []
+        for prec in (0, 1):
+            s = ljgb_mod.System(n=N, density=rho, temperature=1.0, canonical=canonical, precision=prec)
+            s.set_state(pos, vel)
+            s.calculate_forces()
+            s.integrate(0.004, 15)
+            s.integrate(0.004, 15)
+            out.append((s.get_state(), s.observables()))
+        (p0, v0, f0), o0 = out[0]
+        (p1, v1, f1), o1 = out[1]
+        assert np.abs(p0 - p1).max() < 1e-6 * L
+        assert np.abs(v0 - v1).max() < 1e-5
+        for k in ("K", "V", "T", "P", "U", "t"):
+            assert o0[k] == pytest.approx(o1[k], rel=1e-6, abs=1e-6), (canonical, k)
+        assert o0["step"] == o1["step"] == 30 and o0["av_iters"] == o1["av_iters"] == 31
