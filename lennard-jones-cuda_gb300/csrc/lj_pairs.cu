@@ -32,7 +32,24 @@ namespace ljgb {
 
 namespace {
 
-constexpr int kChunk = 16;  // pairs per compensated force partial sum
+#ifndef LJ_CHUNK
+#define LJ_CHUNK 16
+#endif
+constexpr int kChunk = LJ_CHUNK;  // pairs per compensated force partial sum
+
+// Wrapping difference of two fixed-point coordinates.  With LJ_SUB_IMAD the
+// subtraction is issued as an integer multiply-add by a runtime -1 (FMA pipe)
+// instead of an add (ALU pipe), to balance the two pipes.
+__device__ __forceinline__ int fixed_diff(int a, int b, int m1) {
+#ifdef LJ_SUB_IMAD
+  int r;
+  asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(r) : "r"(b), "r"(m1), "r"(a));
+  return r;
+#else
+  (void)m1;
+  return (int)((unsigned)a - (unsigned)b);
+#endif
+}
 
 __device__ __forceinline__ float rcp_approx(float x) {
   float r;
@@ -45,10 +62,10 @@ __device__ __forceinline__ float rcp_approx(float x) {
 template <bool MASKED>
 __device__ __forceinline__ void pair_mixed(const int4 qi, const int4 qj, float k2inv, bool excl,
                                            float& fx, float& fy, float& fz, float& pa,
-                                           float& pb) {
-  const float dx = __int2float_rn((int)((unsigned)qi.x - (unsigned)qj.x));
-  const float dy = __int2float_rn((int)((unsigned)qi.y - (unsigned)qj.y));
-  const float dz = __int2float_rn((int)((unsigned)qi.z - (unsigned)qj.z));
+                                           float& pb, int m1) {
+  const float dx = __int2float_rn(fixed_diff(qi.x, qj.x, m1));
+  const float dy = __int2float_rn(fixed_diff(qi.y, qj.y, m1));
+  const float dz = __int2float_rn(fixed_diff(qi.z, qj.z, m1));
   const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
   // r2 is in fixed-point units^2, between ~1e14 and ~1.4e19: far from the
   // subnormal and 2^126 ranges, so the raw approximate reciprocal applies.
@@ -137,6 +154,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
   int4 qi = a.q[bi.p0 + (valid_i ? i_local : bi.i0)];
   float k2inv = a.sc[bi.sys].k2inv;
   float k2 = a.sc[bi.sys].k2;
+  const int m1 = a.minus_one;
   FloatAcc acc[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
@@ -163,7 +181,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           for (int c0 = 0; c0 < TILE; c0 += kChunk) {
             float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
 #pragma unroll
-            for (int jj = c0; jj < c0 + kChunk; ++jj) pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb);
+            for (int jj = c0; jj < c0 + kChunk; ++jj) pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb, m1);
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);
@@ -175,7 +193,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
             float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
             const int c1 = min(cnt, c0 + kChunk);
             for (int jj = c0; jj < c1; ++jj)
-              pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb);
+              pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb, m1);
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);

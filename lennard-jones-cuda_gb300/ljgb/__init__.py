@@ -127,14 +127,20 @@ def _declare(L):
 
 
 def load(build: bool = True) -> C.CDLL:
-    """Load liblj_gb300.so (building it first when missing or stale)."""
+    """Load liblj_gb300.so (building it first when missing or stale).
+
+    LJGB_LIBRARY=<path> loads another build of the same library instead
+    (for example one compiled with different kernel options)."""
     global _lib
     if _lib is None:
-        if build:
-            _build.build()
-        if not os.path.exists(LIB_PATH):
-            raise OSError("liblj_gb300.so not built: run ljgb.build.build()")
-        L = C.CDLL(LIB_PATH)
+        path = os.environ.get("LJGB_LIBRARY")
+        if path is None:
+            if build:
+                _build.build()
+            path = LIB_PATH
+        if not os.path.exists(path):
+            raise OSError("%s not built: run ljgb.build.build()" % path)
+        L = C.CDLL(path)
         _declare(L)
         _lib = L
     return _lib

@@ -39,8 +39,9 @@ def nvcc() -> str:
 
 
 def _flags():
+    extra = os.environ.get("LJGB_NVCC_FLAGS", "").split()
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE, "-I", CSRC,
-                   "-Xptxas", "-warn-spills"]
+                   "-Xptxas", "-warn-spills"] + extra
 
 
 def _compile(src: str, verbose: bool) -> str:
@@ -68,20 +69,34 @@ def _stale() -> bool:
     return os.path.getmtime(os.path.abspath(__file__)) > t
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile the CUDA/C++ sources into liblj_gb300.so (skipped when fresh)."""
-    if not force and not _stale():
+def build(force: bool = False, verbose: bool = False, out: str = None, build_dir: str = None) -> str:
+    """Compile the CUDA/C++ sources into liblj_gb300.so (skipped when fresh).
+
+    out / build_dir place a variant build elsewhere (extra nvcc flags come
+    from LJGB_NVCC_FLAGS)."""
+    global BUILD_DIR
+    lib_path = out or LIB_PATH
+    if out is None and not force and not _stale():
         return LIB_PATH
+    saved = BUILD_DIR
+    BUILD_DIR = build_dir or BUILD_DIR
+    try:
+        return _build_into(lib_path, verbose)
+    finally:
+        BUILD_DIR = saved
+
+
+def _build_into(lib_path: str, verbose: bool) -> str:
     os.makedirs(BUILD_DIR, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    tmp = LIB_PATH + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
