@@ -1104,9 +1104,52 @@ lj_status lj_set_kernel_shape(lj_system* s, int32_t shape) {
 
 lj_status lj_autotune(lj_system* s) {
   if (!s) return LJ_ERR_INVALID;
-  if (s->prec == LJ_PREC_FP64) return LJ_OK;
+  if (s->prec == LJ_PREC_FP64) return LJ_OK;  // one FP64 shape
   cudaSetDevice(s->device);
-  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  lj_status st = check_status(s);
+  if (st) return st;
+  // Every shape is timed on whole steps of this very system (the fused step
+  // ranks shapes differently from the bare pair kernel); the state is
+  // snapshotted first and restored after each trial.
+  const size_t n3 = 3 * (size_t)s->npad;
+  std::vector<DevBuf<double>> snap(6);
+  DevBuf<int4> snap_q, snap_q2;
+  DevBuf<DevScalars> snap_sc;
+  DevBuf<DevRecord> snap_rec;
+  double* cur[6] = {s->x.p, s->v.p, s->f.p, s->tf.p, s->e.p, s->w.p};
+  const size_t cnt[6] = {n3, n3, n3, n3, (size_t)s->npad, (size_t)s->npad};
+  for (int k = 0; k < 6; ++k) {
+    LJ_CUDA(s, snap[k].alloc(cnt[k]));
+    LJ_CUDA(s, cudaMemcpyAsync(snap[k].p, cur[k], sizeof(double) * cnt[k], cudaMemcpyDeviceToDevice, s->stream));
+  }
+  LJ_CUDA(s, snap_q.alloc(s->npad));
+  LJ_CUDA(s, snap_q2.alloc(s->npad));
+  LJ_CUDA(s, snap_sc.alloc(s->nsys));
+  LJ_CUDA(s, cudaMemcpyAsync(snap_q.p, s->q.p, sizeof(int4) * s->npad, cudaMemcpyDeviceToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(snap_q2.p, s->q2.p, sizeof(int4) * s->npad, cudaMemcpyDeviceToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(snap_sc.p, s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToDevice, s->stream));
+  if (s->rec_cap > 0) {
+    LJ_CUDA(s, snap_rec.alloc(s->records.n));
+    LJ_CUDA(s, cudaMemcpyAsync(snap_rec.p, s->records.p, sizeof(DevRecord) * s->records.n, cudaMemcpyDeviceToDevice,
+                               s->stream));
+  }
+  const int qpar = s->qpar;
+  const bool was_profiling = s->profiling;
+  s->profiling = false;
+  auto restore = [&]() -> lj_status {
+    for (int k = 0; k < 6; ++k)
+      LJ_CUDA(s, cudaMemcpyAsync(cur[k], snap[k].p, sizeof(double) * cnt[k], cudaMemcpyDeviceToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(s->q.p, snap_q.p, sizeof(int4) * s->npad, cudaMemcpyDeviceToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(s->q2.p, snap_q2.p, sizeof(int4) * s->npad, cudaMemcpyDeviceToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(s->sc.p, snap_sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->rec_cap > 0)
+      LJ_CUDA(s, cudaMemcpyAsync(s->records.p, snap_rec.p, sizeof(DevRecord) * s->records.n,
+                                 cudaMemcpyDeviceToDevice, s->stream));
+    LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+    s->qpar = qpar;
+    return LJ_OK;
+  };
+  double dt = s->boxes[0].dt > 0 ? s->boxes[0].dt : 0.005;
   cudaEvent_t e0, e1;
   LJ_CUDA(s, cudaEventCreate(&e0));
   LJ_CUDA(s, cudaEventCreate(&e1));
@@ -1114,15 +1157,13 @@ lj_status lj_autotune(lj_system* s) {
   float best_ms = 1e30f;
   for (int k = 0; k < kNumShapes; ++k) {
     s->shape = k;
-    lj_status st = setup_schedule(s);
-    if (st) return st;
-    if ((st = enqueue_frame_all(s))) return st;
-    for (int w = 0; w < 2; ++w)
-      if ((st = enqueue_pairs(s, true, false, nullptr))) return st;
+    if ((st = setup_schedule(s))) return st;
+    if ((st = restore())) return st;
+    if ((st = enqueue_compute_forces(s))) return st;
+    if ((st = lj_step(s, dt, 2))) return st;
     LJ_CUDA(s, cudaEventRecord(e0, s->stream));
-    const int reps = 5;
-    for (int r = 0; r < reps; ++r)
-      if ((st = enqueue_pairs(s, true, false, nullptr))) return st;
+    const int reps = 6;
+    if ((st = lj_step(s, dt, reps))) return st;
     LJ_CUDA(s, cudaEventRecord(e1, s->stream));
     LJ_CUDA(s, cudaEventSynchronize(e1));
     float ms = 0;
@@ -1137,9 +1178,15 @@ lj_status lj_autotune(lj_system* s) {
   cudaEventDestroy(e1);
   s->shape = best;
   s->tuned = true;
-  lj_status st = setup_schedule(s);
-  if (st) return st;
-  return enqueue_compute_forces(s);
+  s->profiling = was_profiling;
+  if ((st = setup_schedule(s))) return st;
+  if ((st = restore())) return st;
+  // The restored shadow and sums belong to the old i-block length: rebuild
+  // forces, then put back the observables and running sums.
+  if ((st = enqueue_compute_forces(s))) return st;
+  LJ_CUDA(s, cudaMemcpyAsync(s->sc.p, snap_sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToDevice, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LJ_OK;
 }
 
 lj_status lj_profile_enable(lj_system* s, int32_t on) {

@@ -209,3 +209,22 @@ def test_fused_matches_unfused_path(ljgb_mod):
         for k in ("K", "V", "T", "P", "U", "t"):
             assert o0[k] == pytest.approx(o1[k], rel=1e-6, abs=1e-6), (canonical, k)
         assert o0["step"] == o1["step"] == 30 and o0["av_iters"] == o1["av_iters"] == 31
+
+
+def test_autotune_keeps_the_state(ljgb_mod):
+    s = ljgb_mod.System(n=2000, density=0.85, temperature=1.0, canonical=1, lattice=1, jitter=0.02)
+    s.set_recording(8)
+    s.integrate(0.005, 5)
+    p0, v0, f0 = s.get_state()
+    o0 = s.observables()
+    r0 = s.records()
+    s.autotune()
+    p1, v1, f1 = s.get_state()
+    o1 = s.observables()
+    assert np.array_equal(p0, p1) and np.array_equal(v0, v1)
+    assert np.abs(f0 - f1).max() <= 1e-5 * np.abs(f0).max()   # recomputed with the chosen shape
+    for k in ("t", "step", "av_iters", "av_U_tot", "av_p_tot", "av_T_tot", "K", "U"):
+        assert o0[k] == o1[k], k
+    assert s.records() == r0
+    s.integrate(0.005, 3)
+    assert s.observables()["step"] == 8
