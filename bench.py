@@ -219,7 +219,7 @@ def fp32_peak_nominal(device):
 
 def read_traffic():
     """Per-launch DRAM bytes of the pair kernel from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "pairs_mixed_n16384_ncu.md")
+    path = os.path.join(REPO, "profiles", "pairs_mixed_fused_n16384_ncu.md")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch:"):

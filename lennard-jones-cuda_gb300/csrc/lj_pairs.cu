@@ -170,7 +170,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     const int cnt = min(TILE, bi.n_sys - j0);
     if (ok) {
       const int4* st = sq + s * TILE;
-      const bool masked = (cnt < TILE) || (j0 < bi.i0 + bi.n_i && j0 + cnt > bi.i0);
+      const bool masked = j0 < bi.i0 + bi.n_i && j0 + cnt > bi.i0;  // tile holds this block's own i's
       if (FORCES) {
         // Force sums are folded into the TwoSum accumulators every kChunk
         // pairs, so a large near-neighbour term rounds at most kChunk-1 later
@@ -178,12 +178,24 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
         // chunk partial is never small next to the tile sum, so the far-field
         // (s/r)^6 tail is not truncated.
         float ta = 0.f, tb = 0.f;
-        if (!masked) {
+        if (cnt == TILE) {
+          // Full tile: unrolled chunks.  Only the diagonal tile (the j-range
+          // holding this CTA's own i's) needs the self-pair excluded; it
+          // keeps the unrolled loop and pays one compare + select per pair.
+          const bool diag = masked;
 #pragma unroll 1
           for (int c0 = 0; c0 < TILE; c0 += kChunk) {
             float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
+            if (!diag) {
 #pragma unroll
-            for (int jj = c0; jj < c0 + kChunk; ++jj) pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb, m1);
+              for (int jj = c0; jj < c0 + kChunk; ++jj)
+                pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb, m1);
+            } else {
+              const int self = i_local - j0;  // tile-local index of this thread's i
+#pragma unroll
+              for (int jj = c0; jj < c0 + kChunk; ++jj)
+                pair_mixed<true>(qi, st[jj], k2inv, jj == self, fx, fy, fz, pa, pb, m1);
+            }
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);
@@ -191,6 +203,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
             tb += pb;
           }
         } else {
+          // Ragged last tile of a box.
           for (int c0 = 0; c0 < cnt; c0 += kChunk) {
             float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
             const int c1 = min(cnt, c0 + kChunk);
@@ -481,8 +494,8 @@ cudaError_t occupancy_fp64_t(int* blocks_per_sm) {
   X(1, 64, 256, 3, 16)  \
   X(2, 256, 256, 3, 4)  \
   X(3, 128, 512, 2, 8)  \
-  X(4, 128, 256, 3, 10) \
-  X(5, 256, 256, 3, 5)
+  X(4, 128, 512, 3, 8)  \
+  X(5, 256, 512, 3, 4)
 
 const PairShape kShapes[] = {
 #define LJ_SHAPE_ROW(i, T, TL, S, M) {T, TL, S},
