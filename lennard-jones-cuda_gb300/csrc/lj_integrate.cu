@@ -319,7 +319,7 @@ __global__ void k_tvn_finish(StateArgs s) {
 // CalculateParameters (MDSystem.cpp:325-359) per box (one CTA per box).
 template <int MODE>
 __global__ void k_observables(StateArgs s) {
-  __shared__ double sh[32];
+  __shared__ double sh[3 * 32];
   observables_box<MODE>(s, blockIdx.x, sh);
 }
 
@@ -344,8 +344,11 @@ __global__ void k_predict(StateArgs s) {
 // chi dt tF, boundaries, K, the next step's predictor, and -- in the last
 // CTA to finish -- the observables of every box.
 __global__ void k_tvn_close(StateArgs s) {
-  __shared__ double sh[32];
+  __shared__ double sh[3 * 32];
   __shared__ int last;
+  // Launched as a programmatic dependent of the pair kernel: the CTAs start
+  // while the pair grid drains and wait here until its writes are visible.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int B = blockIdx.x;
   const BlockInfo bi = s.blocks[B];
   const int tid = threadIdx.x;
@@ -515,8 +518,17 @@ cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t
 }
 
 cudaError_t launch_tvn_close(const StateArgs& s, int nblocks, int bi, cudaStream_t st) {
-  k_tvn_close<<<nblocks, bi, 0, st>>>(s);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(bi);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_tvn_close, s);
 }
 
 cudaError_t launch_velocity_hist(const StateArgs& s, int nblocks, int bi, double step, int nb,

@@ -295,6 +295,9 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     }
   }
 
+  // The dependent kernel of a fused TVN step (k_tvn_close) may be scheduled
+  // from here on; it waits for this grid's completion before reading.
+  if (EPI == MODE_TVN) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   if (failed) {
     // Drain the copies still in flight before the CTA's shared memory goes away.
     if (tid == 0) {

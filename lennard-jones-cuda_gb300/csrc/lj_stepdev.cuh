@@ -42,16 +42,32 @@ __device__ __forceinline__ double box_sum(const StateArgs& s, int b0, int b1, in
   return acc[0];
 }
 
+// Sums of blk_part[b][0..2] (K, V, W) over the blocks of one box in one
+// block reduction (fixed order); valid in thread 0.  sh: 3 x 32 doubles.
+__device__ __forceinline__ void box_sum3(const StateArgs& s, int b0, int b1, double* sh, double (&out)[3]) {
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int b = b0 + (int)threadIdx.x; b < b1; b += blockDim.x) {
+    const double* bp = s.blk_part + (size_t)b * 8;
+    acc[0] += __ldcg(bp);
+    acc[1] += __ldcg(bp + 1);
+    acc[2] += __ldcg(bp + 2);
+  }
+  block_sum<3>(acc, sh);
+  out[0] = acc[0];
+  out[1] = acc[1];
+  out[2] = acc[2];
+}
+
 // CalculateParameters (MDSystem.cpp:325-359) for box `sys`, plus t += dt for
 // steps (MDSystem.cpp:582) and the optional per-step record.  Block-wide call;
-// thread 0 writes.
+// thread 0 writes.  sh: 3 x 32 doubles.
 template <int MODE>
 __device__ __forceinline__ void observables_box(const StateArgs& s, int sys, double* sh) {
   const BoxArgs box = s.boxes[sys];
   const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
-  const double K = box_sum(s, b0, b1, 0, sh);
-  const double V = box_sum(s, b0, b1, 1, sh);
-  const double W = box_sum(s, b0, b1, 2, sh);
+  double kvw[3];
+  box_sum3(s, b0, b1, sh, kvw);
+  const double K = kvw[0], V = kvw[1], W = kvw[2];
   if (threadIdx.x != 0) return;
   DevScalars& sc = s.sc[sys];
   const double N = (double)box.N;
@@ -130,6 +146,7 @@ __device__ __forceinline__ void fused_block_step(const StateArgs& s, int B, doub
   double part[4] = {0., 0., 0., 0.};
   if (valid) {
     double S[5] = {0., 0., 0., 0., 0.};
+#pragma unroll 4
     for (int k = 0; k < bi.seg_count; ++k) {
       const size_t base = (size_t)(bi.seg_first + k) * 5 * s.bi_threads + tid;
 #pragma unroll
