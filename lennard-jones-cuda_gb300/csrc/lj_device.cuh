@@ -13,23 +13,27 @@ namespace ljgb {
 // ---------------------------------------------------------------------------
 // Fixed-point shadow positions.
 //
-// A coordinate x is stored as q = 3 * rint(frac((x - origin)/P) * 2^32 / 3)
-// (int32 bits, at most 2^32 - 1).  For a periodic box P = L and origin = 0:
-// the 32-bit wrapping difference qi - qj is then exactly the minimum-image
-// separation in units of L/2^32, the role lround(r/L) plays in
-// MDSystem.cu:31-33 and fast_round in MDSystem.cpp:273-277.  Keeping q on
+// A coordinate x is stored as the int32 bits of u = llrint((x - origin) *
+// 2^32 / P) mod 2^32, moved to the nearest multiple of 3.  For a periodic box
+// P = L and origin = 0: the 32-bit wrapping difference qi - qj is then exactly
+// the minimum-image separation in units of L/2^32, the role lround(r/L) plays
+// in MDSystem.cu:31-33 and fast_round in MDSystem.cpp:273-277 (taking the low
+// 32 bits of the rounded integer is the wrap into the box).  Keeping q on
 // multiples of 3 makes a difference of exactly 2^31 (a separation of exactly
 // L/2, where both images are equally near) impossible, since 3 does not
 // divide 2^31; every ordered pair therefore sees the exact negative of its
 // partner's separation, as the reference's antisymmetric rounding does.  The
 // grid is 3 L/2^32 (2e-8 sigma at L = 27 sigma).  For walls / open boxes P is
 // chosen at least twice the particle extent so no difference wraps.
+// Cost: one FP64 multiply, one conversion and a few integer operations (FP64
+// runs at 1/64 of the FP32 rate on this part).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int32_t fixed_coord(double x, double origin, double invP) {
-  double f = (x - origin) * invP;
-  f = f - floor(f);
-  const double q = 3.0 * rint(f * (4294967296.0 / 3.0));
-  return (int32_t)(uint32_t)(uint64_t)q;
+  const double t = (x - origin) * (invP * 4294967296.0);
+  const uint32_t u = (uint32_t)(unsigned long long)llrint(t);
+  const uint32_t r = u % 3u;
+  const uint32_t q = r == 0u ? u : (r == 1u ? u - 1u : u + 1u);
+  return (int32_t)q;
 }
 
 // ---------------------------------------------------------------------------

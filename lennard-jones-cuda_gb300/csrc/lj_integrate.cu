@@ -207,13 +207,12 @@ __global__ void k_reduce(StateArgs s) {
   double part[4] = {0., 0., 0., 0.};
   if (valid) {
     double S[5] = {0., 0., 0., 0., 0.};
-    for (int k = 0; k < bi.seg_count; ++k) {
-      const size_t base = (size_t)(bi.seg_first + k) * 5 * s.bi_threads + tid;
-      if (PREC == 0) {
-#pragma unroll
-        for (int c = 0; c < 5; ++c) S[c] += (double)s.partial[base + (size_t)c * s.bi_threads];
-      } else {
-        const double* pd = reinterpret_cast<const double*>(s.partial);
+    if (PREC == 0) {
+      segment_sums(s, bi, tid, S);
+    } else {
+      const double* pd = reinterpret_cast<const double*>(s.partial);
+      for (int k = 0; k < bi.seg_count; ++k) {
+        const size_t base = (size_t)(bi.seg_first + k) * 5 * s.bi_threads + tid;
 #pragma unroll
         for (int c = 0; c < 5; ++c) S[c] += pd[base + (size_t)c * s.bi_threads];
       }

@@ -123,6 +123,24 @@ __device__ __forceinline__ void tvn_chi_box(const StateArgs& s, int sys, double*
   }
 }
 
+// Sum of a particle's pair-kernel segments (5 values each).  The partials are
+// FP32 values carrying TwoSum-compensated sums; they are added here in FP32
+// TwoSum too (exact up to the low word's rounding) and converted to FP64 once,
+// instead of ~10 conversions and additions per value on the FP64 pipe.
+__device__ __forceinline__ void segment_sums(const StateArgs& s, const BlockInfo& bi, int tid, double (&S)[5]) {
+  FloatAcc acc[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
+#pragma unroll 4
+  for (int k = 0; k < bi.seg_count; ++k) {
+    const size_t base = (size_t)(bi.seg_first + k) * 5 * s.bi_threads + tid;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) two_sum_add(acc[c], __ldcg(s.partial + base + (size_t)c * s.bi_threads));
+  }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) S[c] = (double)acc[c].hi + (double)acc[c].lo;
+}
+
 // Fused second half of a step for block B, run by the CTA that wrote the last
 // pair-kernel segment of the block (blockDim.x = the i-block length).
 // Starts from the state at the beginning of the step (x_n, v_n, F_n); the
@@ -145,13 +163,8 @@ __device__ __forceinline__ void fused_block_step(const StateArgs& s, int B, doub
   const double dt = box.dt;
   double part[4] = {0., 0., 0., 0.};
   if (valid) {
-    double S[5] = {0., 0., 0., 0., 0.};
-#pragma unroll 4
-    for (int k = 0; k < bi.seg_count; ++k) {
-      const size_t base = (size_t)(bi.seg_first + k) * 5 * s.bi_threads + tid;
-#pragma unroll
-      for (int c = 0; c < 5; ++c) S[c] += (double)__ldcg(s.partial + base + (size_t)c * s.bi_threads);
-    }
+    double S[5];
+    segment_sums(s, bi, tid, S);
     const double fs = sc.fscale;
     const double Fn1[3] = {fs * S[0], fs * S[1], fs * S[2]};
     const double e = 4.0 * box.eps * (S[3] - S[4]);

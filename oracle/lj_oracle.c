@@ -468,14 +468,14 @@ void f64_step(f64_state* s, double dt) {
 /* Part 3: emulation of the device's integer decisions (exact histograms).   */
 /* ------------------------------------------------------------------------ */
 
-/* Device shadow: a periodic coordinate as a 32-bit fraction of the box on a
- * grid of 3 units, q = 3 * rint(frac(x/L) * 2^32 / 3) (<= 2^32 - 1).  The
- * device computes exactly this in FP64 (floor, scale, round-to-nearest-even). */
+/* Device shadow: a periodic coordinate as the low 32 bits of
+ * llrint(x * 2^32 / L), moved to the nearest multiple of 3 -- the device's
+ * arithmetic (one double multiply by invL * 2^32, round to nearest even). */
 uint32_t emu_fixed_coord(double x, double invL) {
-  double f = x * invL;
-  f = f - floor(f);
-  double q = 3.0 * rint(f * (4294967296.0 / 3.0));
-  return (uint32_t)q;
+  const double t = x * (invL * 4294967296.0);
+  const uint32_t u = (uint32_t)(unsigned long long)llrint(t);
+  const uint32_t r = u % 3u;
+  return r == 0u ? u : (r == 1u ? u - 1u : u + 1u);
 }
 
 /* r^2 of a pair in box units^2 exactly as the device forms it in FP32:

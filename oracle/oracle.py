@@ -248,13 +248,14 @@ class F64System:
 # Device-decision emulation (exact histogram parity)
 # --------------------------------------------------------------------------
 def emu_fixed(pos, L):
-    """FP64 positions -> uint32 fractions of the box on the device's grid of 3
-    units: q = 3 * rint(frac(x/L) * 2^32 / 3)."""
+    """FP64 positions -> the device's uint32 shadow: low 32 bits of
+    rint(x * (1/L) * 2^32), moved to the nearest multiple of 3."""
     pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
-    f = pos * (1.0 / L)
-    f = f - np.floor(f)
-    q = 3.0 * np.rint(f * (4294967296.0 / 3.0))
-    return q.astype(np.uint64).astype(np.uint32)
+    scale = (1.0 / L) * 4294967296.0
+    u = (np.rint(pos * scale).astype(np.int64) & 0xFFFFFFFF).astype(np.uint64)
+    r = u % 3
+    q = np.where(r == 0, u, np.where(r == 1, u - 1, u + 1))
+    return q.astype(np.uint32)
 
 
 def emu_rdf_r2(q, k2, inv_dr2, nb=256, mode=0, nthreads=None):
