@@ -125,18 +125,31 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
   const int ntiles = t1 - t0;
   if (ntiles <= 0) return;
 
+  // Barrier-free j-tile pipeline: warps wait only for the data of the stage
+  // they read (its mbarrier) and count themselves done with it in shared
+  // memory; the last warp to finish a stage refills it with the tile STAGES
+  // ahead (its lane 0 issues the bulk copy).  Warps therefore drift freely by
+  // up to STAGES-1 tiles instead of meeting at a CTA barrier every tile.
+  constexpr int NW = THREADS / 32;
+  __shared__ int done_cnt[STAGES];
+  __shared__ int prod[3];  // producer cursor: i-block, j-tile, tiles issued
+  __shared__ volatile int sfail;
+  const int lane = tid & 31;
+
   if (HIST) {
     for (int b = tid; b < a.hist.nb; b += THREADS) shist[b] = 0u;
   }
   if (tid == 0) {
-    for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&bars[s], 1);
+      done_cnt[s] = 0;
+    }
+    sfail = 0;
     fence_mbar_init();
   }
   __syncthreads();
-
-  // Producer cursor (thread 0): next tile to copy.
-  int pB = a.cta_block[g], pjt = a.cta_jt[g], issued = 0;
   if (tid == 0) {
+    int pB = a.cta_block[g], pjt = a.cta_jt[g], issued = 0;
     const int pre = ntiles < STAGES ? ntiles : STAGES;
     for (; issued < pre; ++issued) {
       const BlockInfo bi = a.blocks[pB];
@@ -147,7 +160,11 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
       bulk_g2s(sq + s * TILE, a.q + bi.p0 + j0, (uint32_t)cnt * 16u, &bars[s]);
       if (++pjt == bi.njt) { ++pB; pjt = 0; }
     }
+    prod[0] = pB;
+    prod[1] = pjt;
+    prod[2] = issued;
   }
+  __syncthreads();
 
   int B = a.cta_block[g], jt = a.cta_jt[g];
   BlockInfo bi = a.blocks[B];
@@ -161,14 +178,24 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
 #pragma unroll
   for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
 
-  int k = 0;
+  // A warp whose wait times out (or that sees another warp's timeout) keeps
+  // walking the tile sequence without computing, so every CTA-wide barrier
+  // below is still reached by all warps; results of the launch are void.
   bool failed = false;
-  for (; k < ntiles; ++k) {
+  for (int k = 0; k < ntiles; ++k) {
     const int s = k % STAGES;
-    const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((k / STAGES) & 1));
+    if (!failed) {
+      const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], (uint32_t)((k / STAGES) & 1)));
+      if (!ok) {
+        failed = true;
+        if (lane == 0) sfail = 1;
+      } else if (sfail) {
+        failed = true;
+      }
+    }
     const int j0 = jt * TILE;
     const int cnt = min(TILE, bi.n_sys - j0);
-    if (ok) {
+    if (!failed) {
       const int4* st = sq + s * TILE;
       const bool masked = j0 < bi.i0 + bi.n_i && j0 + cnt > bi.i0;  // tile holds this block's own i's
       if (FORCES) {
@@ -227,24 +254,32 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
         }
       }
     }
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
-    }
-    // Stage s is free again: refill it with the tile STAGES ahead.
-    if (tid == 0 && issued < ntiles) {
-      const BlockInfo pbi = a.blocks[pB];
-      const int pj0 = pjt * TILE;
-      const int pcnt = min(TILE, pbi.n_sys - pj0);
-      mbar_arrive_expect_tx(&bars[s], (uint32_t)pcnt * 16u);
-      bulk_g2s(sq + s * TILE, a.q + pbi.p0 + pj0, (uint32_t)pcnt * 16u, &bars[s]);
-      if (++pjt == pbi.njt) { ++pB; pjt = 0; }
-      ++issued;
+    // This warp is done reading stage s; the last warp done refills it.
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      if (atomicAdd(&done_cnt[s], 1) == NW - 1) {
+        done_cnt[s] = 0;
+        const int issued = prod[2];
+        if (issued < ntiles) {
+          const int pB = prod[0], pjt = prod[1];
+          const BlockInfo pbi = a.blocks[pB];
+          const int pj0 = pjt * TILE;
+          const int pcnt = min(TILE, pbi.n_sys - pj0);
+          mbar_arrive_expect_tx(&bars[s], (uint32_t)pcnt * 16u);
+          bulk_g2s(sq + s * TILE, a.q + pbi.p0 + pj0, (uint32_t)pcnt * 16u, &bars[s]);
+          const bool wrap = (pjt + 1 == pbi.njt);
+          prod[0] = wrap ? pB + 1 : pB;
+          prod[1] = wrap ? 0 : pjt + 1;
+          prod[2] = issued + 1;
+        }
+        __threadfence_block();
+      }
     }
     const bool last = (k == ntiles - 1);
     const bool block_end = (jt + 1 == bi.njt);
     if (block_end || last) {
-      if (FORCES && valid_i) {
+      if (FORCES && valid_i && !failed) {
         const int seg = bi.seg_first + (g - bi.g_first);
         float* out = a.partial + (size_t)seg * 5 * THREADS;
 #pragma unroll
@@ -257,7 +292,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
         // completes the count owns the block's epilogue)
         __threadfence();
         __syncthreads();
-        if (tid == 0) sflag = (atomicAdd(st.blk_cnt + B, 1) == bi.seg_count - 1);
+        if (tid == 0) sflag = !sfail && (atomicAdd(st.blk_cnt + B, 1) == bi.seg_count - 1);
         __syncthreads();
         if (sflag) {
           __threadfence();
@@ -298,10 +333,13 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
   // The dependent kernel of a fused TVN step (k_tvn_close) may be scheduled
   // from here on; it waits for this grid's completion before reading.
   if (EPI == MODE_TVN) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  if (failed) {
+  __syncthreads();
+  if (sfail) {
     // Drain the copies still in flight before the CTA's shared memory goes away.
     if (tid == 0) {
-      for (int kk = k; kk < issued; ++kk) mbar_wait_bounded(&bars[kk % STAGES], (uint32_t)((kk / STAGES) & 1));
+      const int issued = prod[2];
+      for (int kk = issued - STAGES < 0 ? 0 : issued - STAGES; kk < issued; ++kk)
+        mbar_wait_bounded(&bars[kk % STAGES], (uint32_t)((kk / STAGES) & 1));
       atomicOr(a.status, LJ_DEVFLAG_TIMEOUT);
     }
     return;
