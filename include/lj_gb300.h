@@ -239,11 +239,14 @@ lj_status lj_sample_initial_state(const lj_config* cfg, double* pos, double* vel
 
 /* The stream-K work split the pair kernel uses for boxes n[0..nsys) with
  * i-blocks of `block` particles, j-tiles of `tile` and at most `ctas` CTAs.
- * Writes the CTA count, the number of partial segments, the CTA tile ranges
- * (ctas+1 entries) and, per i-block, 8 ints: box, first particle, particles,
- * box offset, j-tiles, first segment, segments, first CTA. */
+ * Writes the CTA count, the number of partial segments, the CTA ranges
+ * (ctas+1 entries each: CTA g covers j from offset cta_lo[g] of flattened
+ * tile cta_tile_begin[g] up to offset cta_lo[g+1] of tile
+ * cta_tile_begin[g+1], offsets multiples of 32; cta_lo may be NULL) and, per
+ * i-block, 8 ints: box, first particle, particles, box offset, j-tiles, first
+ * segment, segments, first CTA. */
 lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_t tile, int32_t ctas,
-                           int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin,
+                           int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin, int32_t* cta_lo,
                            int32_t* block_info, int32_t max_blocks);
 
 /* All-pairs LJ forces for callers that cannot allocate device memory (code

@@ -142,7 +142,7 @@ struct CompatCtx {
   int4* q = nullptr;
   DevScalars* sc = nullptr;
   BlockInfo* blocks = nullptr;
-  int *ctb = nullptr, *cb = nullptr, *cj = nullptr;
+  int *ctb = nullptr, *clo = nullptr, *cb = nullptr, *cj = nullptr;
   float* partial = nullptr;
   double* blk = nullptr;
   unsigned long long* hist = nullptr;
@@ -154,6 +154,7 @@ struct CompatCtx {
     cudaFree(sc);
     cudaFree(blocks);
     cudaFree(ctb);
+    cudaFree(clo);
     cudaFree(cb);
     cudaFree(cj);
     cudaFree(partial);
@@ -208,6 +209,7 @@ bool ensure_ctx(int n, int block_hint) {
   REF_CHECK(cudaMalloc(&c.sc, sizeof(DevScalars)));
   REF_CHECK(cudaMalloc(&c.blocks, sizeof(BlockInfo) * nb));
   REF_CHECK(cudaMalloc(&c.ctb, sizeof(int) * (s.G + 1)));
+  REF_CHECK(cudaMalloc(&c.clo, sizeof(int) * (s.G + 1)));
   REF_CHECK(cudaMalloc(&c.cb, sizeof(int) * s.G));
   REF_CHECK(cudaMalloc(&c.cj, sizeof(int) * s.G));
   REF_CHECK(cudaMalloc(&c.partial, sizeof(float) * (size_t)s.nseg * 5 * s.BI));
@@ -219,6 +221,7 @@ bool ensure_ctx(int n, int block_hint) {
   REF_CHECK(cudaMemset(c.status, 0, sizeof(int)));
   REF_CHECK(cudaMemcpy(c.blocks, s.blocks.data(), sizeof(BlockInfo) * nb, cudaMemcpyHostToDevice));
   REF_CHECK(cudaMemcpy(c.ctb, s.cta_tile_begin.data(), sizeof(int) * (s.G + 1), cudaMemcpyHostToDevice));
+  REF_CHECK(cudaMemcpy(c.clo, s.cta_lo.data(), sizeof(int) * (s.G + 1), cudaMemcpyHostToDevice));
   REF_CHECK(cudaMemcpy(c.cb, s.cta_block.data(), sizeof(int) * s.G, cudaMemcpyHostToDevice));
   REF_CHECK(cudaMemcpy(c.cj, s.cta_jt.data(), sizeof(int) * s.G, cudaMemcpyHostToDevice));
   c.sched = std::move(s);
@@ -248,6 +251,7 @@ bool calc_forces(float* Pos, float* Force, float* host_pressure, int n, float L,
   a.q = c.q;
   a.blocks = c.blocks;
   a.cta_tile_begin = c.ctb;
+  a.cta_lo = c.clo;
   a.cta_block = c.cb;
   a.cta_jt = c.cj;
   a.sc = c.sc;

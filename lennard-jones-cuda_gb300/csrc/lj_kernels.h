@@ -30,6 +30,8 @@ struct PairArgs {
   const int* cta_tile_begin;  // G+1 tile ranges
   const int* cta_block;       // first i-block of each CTA
   const int* cta_jt;          // first j-tile (within that block) of each CTA
+  const int* cta_lo;          // G+1 j offsets within the first tile (entry g+1: end in the
+                              // last tile, 0 = whole tile); nullptr = whole tiles only
   const DevScalars* sc;       // per box frame / scalars
   const BoxArgs* boxes;       // per box constants
   float* partial;             // nseg x 5 x threads  (float, or double for FP64)

@@ -317,6 +317,7 @@ extern "C" lj_status lj_forces_static(const float* pos4, float* force4, double* 
   a.q = q;
   a.blocks = blocks;
   a.cta_tile_begin = cta_begin;
+  a.cta_lo = nullptr;  // whole-tile ranges (the plan above cuts on tiles only)
   a.cta_block = cta_block;
   a.cta_jt = cta_jt;
   a.sc = sc;

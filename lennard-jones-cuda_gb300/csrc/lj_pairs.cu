@@ -26,6 +26,7 @@
 
 #include "lj_device.cuh"
 #include "lj_kernels.h"
+#include "lj_schedule.h"
 #include "lj_stepdev.cuh"
 
 namespace ljgb {
@@ -36,6 +37,9 @@ namespace {
 #define LJ_CHUNK 32
 #endif
 constexpr int kChunk = LJ_CHUNK;  // pairs per compensated force partial sum
+// CTA ranges start and end on multiples of kSplitGrain j records inside a
+// tile; the unrolled chunk loop needs those to be whole chunks.
+static_assert(kSplitGrain % kChunk == 0, "schedule cuts must fall on chunk boundaries");
 
 // Wrapping difference of two fixed-point coordinates, issued as an integer
 // multiply-add by a runtime -1 so that it runs on the FMA pipe: the int->float
@@ -121,8 +125,11 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
 
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
+  // This CTA's j range: from offset lo0 of its first tile to offset lo1 of
+  // tile t1 (lo1 = 0: up to the end of tile t1 - 1).
   const int t0 = a.cta_tile_begin[g], t1 = a.cta_tile_begin[g + 1];
-  const int ntiles = t1 - t0;
+  const int lo0 = a.cta_lo ? a.cta_lo[g] : 0, lo1 = a.cta_lo ? a.cta_lo[g + 1] : 0;
+  const int ntiles = t1 - t0 + (lo1 > 0 ? 1 : 0);
   if (ntiles <= 0) return;
 
   // Barrier-free j-tile pipeline: warps wait only for the data of the stage
@@ -195,6 +202,8 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     }
     const int j0 = jt * TILE;
     const int cnt = min(TILE, bi.n_sys - j0);
+    const int jlo = k == 0 ? lo0 : 0;                        // multiples of kChunk
+    const int jhi = (k == ntiles - 1 && lo1 > 0) ? lo1 : cnt;
     if (!failed) {
       const int4* st = sq + s * TILE;
       const bool masked = j0 < bi.i0 + bi.n_i && j0 + cnt > bi.i0;  // tile holds this block's own i's
@@ -211,7 +220,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           // keeps the unrolled loop and pays one compare + select per pair.
           const bool diag = masked;
 #pragma unroll 1
-          for (int c0 = 0; c0 < TILE; c0 += kChunk) {
+          for (int c0 = jlo; c0 < jhi; c0 += kChunk) {
             float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
             if (!diag) {
 #pragma unroll
@@ -231,9 +240,9 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           }
         } else {
           // Ragged last tile of a box.
-          for (int c0 = 0; c0 < cnt; c0 += kChunk) {
+          for (int c0 = jlo; c0 < jhi; c0 += kChunk) {
             float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
-            const int c1 = min(cnt, c0 + kChunk);
+            const int c1 = min(jhi, c0 + kChunk);
             for (int jj = c0; jj < c1; ++jj)
               pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb, m1);
             two_sum_add(acc[0], fx);
@@ -247,7 +256,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
         two_sum_add(acc[4], tb);
       }
       if (HIST && valid_i) {
-        for (int jj = 0; jj < cnt; ++jj) {
+        for (int jj = jlo; jj < jhi; ++jj) {
           if (j0 + jj == i_local) continue;
           const int b = pair_bin(qi, st[jj], k2, a.hist);
           if (b >= 0) atomicAdd(&shist[b], 1u);
@@ -377,7 +386,8 @@ __global__ void __launch_bounds__(THREADS) k_pairs_fp64(PairArgs a) {
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
   const int t0 = a.cta_tile_begin[g], t1 = a.cta_tile_begin[g + 1];
-  const int ntiles = t1 - t0;
+  const int lo0 = a.cta_lo ? a.cta_lo[g] : 0, lo1 = a.cta_lo ? a.cta_lo[g + 1] : 0;
+  const int ntiles = t1 - t0 + (lo1 > 0 ? 1 : 0);
   if (ntiles <= 0) return;
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
@@ -416,9 +426,11 @@ __global__ void __launch_bounds__(THREADS) k_pairs_fp64(PairArgs a) {
     const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((k / STAGES) & 1));
     const int j0 = jt * TILE;
     const int cnt = min(TILE, bi.n_sys - j0);
+    const int jlo = k == 0 ? lo0 : 0;
+    const int jhi = (k == ntiles - 1 && lo1 > 0) ? lo1 : cnt;
     if (ok) {
       const double4_32a* st = sx + s * TILE;
-      for (int jj = 0; jj < cnt; ++jj) {
+      for (int jj = jlo; jj < jhi; ++jj) {
         const double4_32a xj = st[jj];
         double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         if (periodic) {  // nearest image, ties away from zero (fast_round, MDSystem.cpp:732-739)

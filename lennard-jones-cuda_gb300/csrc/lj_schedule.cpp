@@ -6,11 +6,13 @@
 
 namespace ljgb {
 
-bool build_schedule(const int* n, int nsys, int BI, int TILE, int G, int tile_overhead, Schedule* out) {
+bool build_schedule(const int* n, int nsys, int BI, int TILE, int G, int tile_overhead, Schedule* out, int grain) {
   if (!n || nsys < 1 || BI < 1 || TILE < 1 || G < 1 || !out || tile_overhead < 0) return false;
+  if (grain < 1 || TILE % grain != 0) return false;
   Schedule s;
   s.BI = BI;
   s.TILE = TILE;
+  s.grain = grain;
   s.sys_block_first.push_back(0);
   int64_t p0 = 0;
   for (int k = 0; k < nsys; ++k) {
@@ -33,68 +35,76 @@ bool build_schedule(const int* n, int nsys, int BI, int TILE, int G, int tile_ov
   }
   const int nblocks = (int)s.blocks.size();
 
-  // Flattened tile sequence: block-major, j-tile minor.  Cost of a tile = its
-  // j count + a fixed overhead (every thread of the CTA runs each j).
-  std::vector<int64_t> tile_first(nblocks + 1, 0);
-  for (int b = 0; b < nblocks; ++b) tile_first[b + 1] = tile_first[b] + s.blocks[b].njt;
-  if (tile_first[nblocks] > INT32_MAX) return false;
+  // Work units: the j-chunks of `grain` records of every block, block-major.
+  // Chunk c of a block covers j in [c*grain, min((c+1)*grain, n_sys)); its
+  // tile is c*grain / TILE (TILE is a multiple of grain).  Cost of a chunk =
+  // its j count, plus a fixed overhead for each tile a CTA starts.
+  std::vector<int64_t> tile_first(nblocks + 1, 0), chunk_first(nblocks + 1, 0), cost_first(nblocks + 1, 0);
+  for (int b = 0; b < nblocks; ++b) {
+    const BlockInfo& bi = s.blocks[b];
+    tile_first[b + 1] = tile_first[b] + bi.njt;
+    chunk_first[b + 1] = chunk_first[b] + (bi.n_sys + grain - 1) / grain;
+    cost_first[b + 1] = cost_first[b] + (int64_t)bi.n_sys + (int64_t)bi.njt * tile_overhead;
+  }
+  if (tile_first[nblocks] > INT32_MAX || chunk_first[nblocks] > INT32_MAX) return false;
   const int ntiles = (int)tile_first[nblocks];
+  const int64_t nchunks = chunk_first[nblocks];
   s.ntiles = ntiles;
-  std::vector<int64_t> block_cost_first(nblocks + 1, 0);
-  for (int b = 0; b < nblocks; ++b)
-    block_cost_first[b + 1] =
-        block_cost_first[b] + (int64_t)s.blocks[b].n_sys + (int64_t)s.blocks[b].njt * tile_overhead;
-  const int64_t total = block_cost_first[nblocks];
-  auto cost_before = [&](int b, int jt) -> int64_t {
-    const int64_t j = std::min<int64_t>((int64_t)jt * TILE, s.blocks[b].n_sys);
-    return block_cost_first[b] + j + (int64_t)jt * tile_overhead;
+  const int64_t total = cost_first[nblocks];
+  // Cost of the work before chunk c of block b.
+  auto cost_before = [&](int b, int64_t c) -> int64_t {
+    const int64_t j = std::min<int64_t>(c * grain, s.blocks[b].n_sys);
+    return cost_first[b] + j + (c * grain + TILE - 1) / TILE * tile_overhead;
   };
 
-  // At most one CTA per tile, so that every CTA owns at least one tile.
-  G = std::min(G, ntiles);
+  // CTA g starts at the first chunk whose preceding cost reaches g/G of the
+  // total; at most one CTA per chunk, so that every CTA owns some work.
+  G = (int)std::min<int64_t>(G, nchunks);
   s.G = G;
-  std::vector<int> tb(G + 1, 0);
-  {
-    int b = 0, jt = 0;
-    for (int g = 0; g < G; ++g) {
-      const int64_t target = (int64_t)((__int128)total * g / G);
-      while (b < nblocks && cost_before(b, jt) < target) {
-        if (++jt == s.blocks[b].njt) {
-          ++b;
-          jt = 0;
-        }
-      }
-      tb[g] = (b < nblocks) ? (int)tile_first[b] + jt : ntiles;
+  std::vector<int64_t> cb(G + 1, 0);
+  for (int g = 1; g < G; ++g) {
+    const int64_t target = (int64_t)((__int128)total * g / G);
+    int b = (int)(std::upper_bound(cost_first.begin(), cost_first.end(), target) - cost_first.begin()) - 1;
+    b = std::max(0, std::min(b, nblocks - 1));
+    int64_t lo = 0, hi = chunk_first[b + 1] - chunk_first[b];  // smallest c in [lo, hi] with cost >= target
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (cost_before(b, mid) >= target) hi = mid;
+      else lo = mid + 1;
     }
+    cb[g] = chunk_first[b] + lo;
   }
-  tb[0] = 0;
-  for (int g = 1; g < G; ++g) tb[g] = std::max(tb[g], tb[g - 1] + 1);
-  for (int g = 1; g < G; ++g) tb[g] = std::min(tb[g], ntiles - (G - g));
-  tb[G] = ntiles;
-  s.cta_tile_begin = tb;
+  cb[0] = 0;
+  for (int g = 1; g < G; ++g) cb[g] = std::max(cb[g], cb[g - 1] + 1);
+  for (int g = G - 1; g >= 1; --g) cb[g] = std::min(cb[g], nchunks - (G - g));
+  cb[G] = nchunks;
 
-  // (block, jt) of each CTA's first tile.
+  // Start of each CTA as (flattened tile, block, tile in block, offset).
+  s.cta_tile_begin.assign(G + 1, ntiles);
+  s.cta_lo.assign(G + 1, 0);
   s.cta_block.assign(G, 0);
   s.cta_jt.assign(G, 0);
   {
     int b = 0;
     for (int g = 0; g < G; ++g) {
-      while (tile_first[b + 1] <= tb[g]) ++b;
+      while (chunk_first[b + 1] <= cb[g]) ++b;
+      const int64_t j = (cb[g] - chunk_first[b]) * grain;
       s.cta_block[g] = b;
-      s.cta_jt[g] = tb[g] - (int)tile_first[b];
+      s.cta_jt[g] = (int)(j / TILE);
+      s.cta_lo[g] = (int)(j % TILE);
+      s.cta_tile_begin[g] = (int)tile_first[b] + (int)(j / TILE);
     }
   }
 
-  // Segments of block b: the CTAs g whose [tb[g], tb[g+1]) meets the block's
-  // tiles; they are consecutive and non-empty, so the segment of (g, b) is
-  // seg_first[b] + g - g_first[b].
+  // Segments of block b: the CTAs whose chunk ranges meet the block's; they
+  // are consecutive, so the segment of (g, b) is seg_first[b] + g - g_first[b].
   int seg = 0;
   int g = 0;
   for (int b = 0; b < nblocks; ++b) {
-    const int t0 = (int)tile_first[b], t1 = (int)tile_first[b + 1];
-    while (g + 1 < G && tb[g + 1] <= t0) ++g;  // last CTA starting at or before t0
+    const int64_t c0 = chunk_first[b], c1 = chunk_first[b + 1];
+    while (g + 1 < G && cb[g + 1] <= c0) ++g;  // last CTA starting at or before c0
     int gh = g;
-    while (gh + 1 < G && tb[gh + 1] < t1) ++gh;  // last CTA starting before t1
+    while (gh + 1 < G && cb[gh + 1] < c1) ++gh;  // last CTA starting before c1
     s.blocks[b].g_first = g;
     s.blocks[b].seg_first = seg;
     s.blocks[b].seg_count = gh - g + 1;

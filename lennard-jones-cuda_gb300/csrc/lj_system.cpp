@@ -86,7 +86,7 @@ struct lj_system {
   bool pred_ready = false;  // current shadow = predictor x + dt v + dt^2 F/2 for pred_dt
   double pred_dt = 0.0;
   DevBuf<BlockInfo> blocks;
-  DevBuf<int> cta_tile_begin, cta_block, cta_jt, sys_block_first;
+  DevBuf<int> cta_tile_begin, cta_lo, cta_block, cta_jt, sys_block_first;
   DevBuf<DevScalars> sc;
   DevBuf<BoxArgs> dboxes;
   DevBuf<double> blk_part;
@@ -172,6 +172,7 @@ PairArgs pair_args(lj_system* s) {
   a.cta_tile_begin = s->cta_tile_begin.p;
   a.cta_block = s->cta_block.p;
   a.cta_jt = s->cta_jt.p;
+  a.cta_lo = s->cta_lo.p;
   a.sc = s->sc.p;
   a.boxes = s->dboxes.p;
   a.partial = s->partial.p;
@@ -254,6 +255,7 @@ lj_status setup_schedule(lj_system* s) {
   const int nb = nblocks(s);
   LJ_CUDA(s, s->blocks.alloc(nb));
   LJ_CUDA(s, s->cta_tile_begin.alloc(s->sched.G + 1));
+  LJ_CUDA(s, s->cta_lo.alloc(s->sched.G + 1));
   LJ_CUDA(s, s->cta_block.alloc(s->sched.G));
   LJ_CUDA(s, s->cta_jt.alloc(s->sched.G));
   LJ_CUDA(s, s->sys_block_first.alloc(s->nsys + 1));
@@ -269,6 +271,8 @@ lj_status setup_schedule(lj_system* s) {
   LJ_CUDA(s, cudaMemcpyAsync(s->blocks.p, s->sched.blocks.data(), sizeof(BlockInfo) * nb, cudaMemcpyHostToDevice,
                              s->stream));
   LJ_CUDA(s, cudaMemcpyAsync(s->cta_tile_begin.p, s->sched.cta_tile_begin.data(), sizeof(int) * (s->sched.G + 1),
+                             cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(s->cta_lo.p, s->sched.cta_lo.data(), sizeof(int) * (s->sched.G + 1),
                              cudaMemcpyHostToDevice, s->stream));
   LJ_CUDA(s, cudaMemcpyAsync(s->cta_block.p, s->sched.cta_block.data(), sizeof(int) * s->sched.G,
                              cudaMemcpyHostToDevice, s->stream));
@@ -690,6 +694,7 @@ lj_status lj_destroy(lj_system* s) {
   s->glob_cnt.free();
   s->blocks.free();
   s->cta_tile_begin.free();
+  s->cta_lo.free();
   s->cta_block.free();
   s->cta_jt.free();
   s->sys_block_first.free();
@@ -1276,8 +1281,8 @@ lj_status lj_sample_initial_state(const lj_config* cfg, double* pos, double* vel
 }
 
 lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_t tile, int32_t ctas,
-                           int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin, int32_t* block_info,
-                           int32_t max_blocks) {
+                           int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin, int32_t* cta_lo,
+                           int32_t* block_info, int32_t max_blocks) {
   Schedule sch;
   if (!build_schedule(n, nsys, block, tile, ctas, kTileOverhead, &sch))
     return fail(nullptr, LJ_ERR_INVALID, "invalid schedule request");
@@ -1285,6 +1290,8 @@ lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_
   if (out_nseg) *out_nseg = sch.nseg;
   if (cta_tile_begin)
     for (int g = 0; g <= sch.G; ++g) cta_tile_begin[g] = sch.cta_tile_begin[g];
+  if (cta_lo)
+    for (int g = 0; g <= sch.G; ++g) cta_lo[g] = sch.cta_lo[g];
   if (block_info) {
     const int nb = std::min<int>(max_blocks, (int)sch.blocks.size());
     for (int b = 0; b < nb; ++b) {

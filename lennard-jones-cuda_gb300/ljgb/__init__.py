@@ -105,7 +105,7 @@ def _declare(L):
         "lj_host_alloc": (_P, [C.c_size_t]),
         "lj_host_free": (None, [_P]),
         "lj_schedule_plan": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
-                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P, C.c_int32]),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P, _P, C.c_int32]),
         # the reference's own ABI (include/lj_reference_abi.h)
         "allocateArray": (None, [C.POINTER(_P), C.c_int]),
         "deleteArray": (None, [_P]),
@@ -212,10 +212,12 @@ def schedule_plan(n: Sequence[int], block: int, tile: int, ctas: int):
     nseg = C.c_int32()
     nb = int(sum((int(x) + block - 1) // block for x in n))
     ctb = np.zeros(ctas + 1, np.int32)
+    clo = np.zeros(ctas + 1, np.int32)
     info = np.zeros((nb, 8), np.int32)
     _check(load().lj_schedule_plan(n.ctypes.data, len(n), block, tile, ctas, C.byref(G), C.byref(nseg),
-                                   ctb.ctypes.data, info.ctypes.data, nb))
-    return dict(ctas=G.value, nseg=nseg.value, cta_tile_begin=ctb[:G.value + 1].copy(), blocks=info)
+                                   ctb.ctypes.data, clo.ctypes.data, info.ctypes.data, nb))
+    return dict(ctas=G.value, nseg=nseg.value, cta_tile_begin=ctb[:G.value + 1].copy(),
+                cta_lo=clo[:G.value + 1].copy(), blocks=info)
 
 
 class System:

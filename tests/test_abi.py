@@ -108,37 +108,68 @@ def test_initial_speeds_are_maxwellian(ljlib):
 
 
 @pytest.mark.parametrize("n,block,tile,ctas", [
-    ([16384], 128, 256, 1824), ([400], 128, 256, 1824), ([1000, 37, 4000, 200], 64, 256, 608),
-    ([5], 128, 256, 1824), ([262144], 128, 256, 1824), ([777], 256, 512, 300)])
+    ([16384], 128, 256, 1216), ([16384], 128, 256, 1824), ([400], 128, 256, 1824),
+    ([1000, 37, 4000, 200], 64, 256, 608), ([5], 128, 256, 1824), ([262144], 128, 256, 1824),
+    ([777], 256, 512, 300), ([1000, 37, 4000, 200], 128, 512, 2000)])
 def test_schedule_covers_every_pair_once(ljlib, n, block, tile, ctas):
+    """Every (i-block, j) belongs to exactly one CTA, CTA ranges are cut on
+    32-record chunks, each (CTA, block) pair has its own segment in the
+    block's range, and the work per CTA is equal to within about one chunk."""
     import ljgb
+    grain = 32
     s = ljgb.schedule_plan(n, block, tile, ctas)
-    G, ctb, blocks = s["ctas"], s["cta_tile_begin"], s["blocks"]
-    assert G <= ctas and ctb[0] == 0 and np.all(np.diff(ctb) >= 1)
+    G, ctb, clo, blocks = s["ctas"], s["cta_tile_begin"], s["cta_lo"], s["blocks"]
+    assert G <= ctas and ctb[0] == 0 and clo[0] == 0 and clo[G] == 0
     njt = blocks[:, 4]
+    nsys = np.array([n[k] for k in blocks[:, 0]])
     assert ctb[-1] == njt.sum()
-    # every (block, tile) belongs to exactly one CTA, and the segment of (g, b)
-    # = seg_first[b] + g - g_first[b] is unique and inside the block's range
+    assert np.all(clo % grain == 0) and np.all((clo >= 0) & (clo < tile))
     tile_first = np.concatenate([[0], np.cumsum(njt)])
-    seen = set()
-    for g in range(G):
-        for t in range(ctb[g], ctb[g + 1]):
-            b = int(np.searchsorted(tile_first, t, side="right") - 1)
-            seg = blocks[b, 5] + g - blocks[b, 7]
-            assert blocks[b, 5] <= seg < blocks[b, 5] + blocks[b, 6]
-            seen.add((b, seg))
-    assert len({sg for _, sg in seen}) == s["nseg"]
-    # balance: the costliest CTA is within two tiles of the mean
-    cost = []
-    for g in range(G):
-        c = 0
-        for t in range(ctb[g], ctb[g + 1]):
-            b = int(np.searchsorted(tile_first, t, side="right") - 1)
-            jt = t - tile_first[b]
-            nsys = n[blocks[b, 0]]
-            c += min(tile, nsys - jt * tile) + 8
-        cost.append(c)
-    assert max(cost) <= np.mean(cost) + 2 * (tile + 8)
+    chunk_first = np.concatenate([[0], np.cumsum((nsys + grain - 1) // grain)])
+    # global chunk index of each CTA's first j: strictly increasing, 0 .. total
+    bstart = np.searchsorted(tile_first, ctb[:G], side="right") - 1
+    jstart = (ctb[:G] - tile_first[bstart]) * tile + clo[:G]
+    assert np.all(jstart < nsys[bstart])
+    C = np.concatenate([chunk_first[bstart] + jstart // grain, [chunk_first[-1]]])
+    assert C[0] == 0 and np.all(np.diff(C) >= 1)
+    # segments: CTAs meeting block b are g_first .. g_first + seg_count - 1
+    seg_first, seg_count, g_first = blocks[:, 5], blocks[:, 6], blocks[:, 7]
+    assert seg_first[0] == 0 and np.all(seg_first[1:] == seg_first[:-1] + seg_count[:-1])
+    assert s["nseg"] == seg_first[-1] + seg_count[-1]
+    for b in range(len(blocks)):
+        meet = np.nonzero((C[:-1] < chunk_first[b + 1]) & (C[1:] > chunk_first[b]))[0]
+        assert meet[0] == g_first[b] and len(meet) == seg_count[b] and np.all(np.diff(meet) == 1)
+    # the kernel's walk of each CTA (small cases) lands on the same j ranges
+    if G * 8 < 20000:
+        cover = {}
+        for g in range(G):
+            t0, t1, lo0, lo1 = ctb[g], ctb[g + 1], clo[g], clo[g + 1]
+            ntiles = t1 - t0 + (1 if lo1 > 0 else 0)
+            b = int(np.searchsorted(tile_first, t0, side="right") - 1)
+            jt = t0 - tile_first[b]
+            for k in range(ntiles):
+                cnt = min(tile, nsys[b] - jt * tile)
+                jlo = lo0 if k == 0 else 0
+                jhi = lo1 if (k == ntiles - 1 and lo1 > 0) else cnt
+                assert 0 <= jlo < jhi <= cnt
+                cover.setdefault(b, []).append((jt * tile + jlo, jt * tile + jhi))
+                if jt + 1 == njt[b]:
+                    b, jt = b + 1, 0
+                else:
+                    jt += 1
+        for b in range(len(blocks)):
+            iv = sorted(cover[b])
+            assert iv[0][0] == 0 and iv[-1][1] == nsys[b]
+            assert all(iv[k][1] == iv[k + 1][0] for k in range(len(iv) - 1))
+    # balance in cost units (j records + 8 per tile started): within ~2 chunks
+    cost_first = np.concatenate([[0], np.cumsum(nsys + njt * 8)])
+    def cost_at(c):
+        b = np.searchsorted(chunk_first, c, side="right") - 1
+        b = np.minimum(b, len(blocks) - 1)
+        j = np.minimum((c - chunk_first[b]) * grain, nsys[b])
+        return cost_first[b] + j + (j + tile - 1) // tile * 8
+    cost = np.diff(cost_at(C))
+    assert cost.max() <= cost.mean() + 2 * (grain + 8)
 
 
 def test_schedule_rejects_bad_input(ljlib):
