@@ -88,7 +88,6 @@ __global__ void k_drift(StateArgs s) {
   const bool valid = (int)threadIdx.x < bi.n_i;
   const int p = bi.p0 + bi.i0 + threadIdx.x;
   const BoxArgs box = s.boxes[bi.sys];
-  const double dt = box.dt;
   double x[3] = {0., 0., 0.};
   if (valid) {
     double v[3];
@@ -96,11 +95,10 @@ __global__ void k_drift(StateArgs s) {
     for (int c = 0; c < 3; ++c) {
       const size_t k = (size_t)c * s.npad + p;
       const double f = s.f[k];
-      x[c] = s.x[k];
       v[c] = s.v[k];
-      x[c] += dt * v[c] + dt * dt * f / 2.;
+      x[c] = drift_pos(box, s.x[k], v[c], f);
       s.x[k] = x[c];
-      if (MODE == MODE_EVN) s.v[k] = v[c] + dt * f / 2.;
+      if (MODE == MODE_EVN) s.v[k] = fma(box.hdt, f, v[c]);
       if (MODE == MODE_TVN) s.tf[k] = 0.5 * f;
     }
     if (box.bc == 0) store_shadow(s, s.sc[bi.sys], p, x[0], x[1], x[2]);
@@ -219,8 +217,8 @@ __global__ void k_reduce(StateArgs s) {
     }
     const double fs = (PREC == 0) ? s.sc[bi.sys].fscale : 4.0 * box.eps / (box.sigma * box.sigma);
     double F[3] = {fs * S[0], fs * S[1], fs * S[2]};
-    const double e = 4.0 * box.eps * (S[3] - S[4]);
-    const double w = 4.0 * box.eps * (12.0 * S[3] - 6.0 * S[4]);
+    const double e = box.eps4 * (S[3] - S[4]);
+    const double w = box.eps4 * fma(12.0, S[3], -6.0 * S[4]);
     s.e[p] = e;
     s.w[p] = w;
     part[1] = 0.5 * e;
@@ -235,10 +233,9 @@ __global__ void k_reduce(StateArgs s) {
     if (MODE == MODE_FORCES_ONLY) {
       part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     } else if (MODE == MODE_EVN) {
-      const double dt = box.dt;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        v[c] += dt * F[c] / 2.;
+        v[c] = fma(box.hdt, F[c], v[c]);
         x[c] = s.x[(size_t)c * s.npad + p];
       }
       apply_bc(box.bc, box.L, x, v);
@@ -249,15 +246,14 @@ __global__ void k_reduce(StateArgs s) {
       }
       part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     } else {  // TVN
-      const double dt = box.dt;
       double tv2 = 0.0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const size_t k = (size_t)c * s.npad + p;
         const double tf = s.tf[k] + 0.5 * F[c];
         s.tf[k] = tf;
-        const double tv = v[c] + dt * tf / 2.;
-        tv2 += tv * tv;
+        const double tv = fma(box.hdt, tf, v[c]);
+        tv2 = fma(tv, tv, tv2);
       }
       part[3] = tv2;
     }
@@ -281,8 +277,8 @@ __global__ void k_tvn_finish(StateArgs s) {
   const int b0 = s.sys_block_first[bi.sys], b1 = s.sys_block_first[bi.sys + 1];
   const double tv2 = box_sum(s, b0, b1, 3, sh);
   if (tid == 0) {
-    const double Tkin = tv2 * (1. / 3. / box.N);
-    const double chi = sqrt(box.T0 / Tkin);
+    double Tkin;
+    const double chi = tvn_chi(box, tv2, &Tkin);
     chi_sh = chi;
     if (B == b0) {
       s.sc[bi.sys].Tkin = Tkin;
@@ -298,7 +294,7 @@ __global__ void k_tvn_finish(StateArgs s) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t k = (size_t)c * s.npad + p;
-      v[c] = (2. * chi - 1.) * s.v[k] + chi * box.dt * s.tf[k];
+      v[c] = fma(2. * chi - 1., s.v[k], chi * box.dt * s.tf[k]);
       x[c] = s.x[k];
     }
     apply_bc(box.bc, box.L, x, v);
@@ -328,20 +324,22 @@ __global__ void k_predict(StateArgs s) {
   const BlockInfo bi = s.blocks[blockIdx.x];
   if ((int)threadIdx.x >= bi.n_i) return;
   const int p = bi.p0 + bi.i0 + threadIdx.x;
-  const double dt = s.boxes[bi.sys].dt;
+  const BoxArgs box = s.boxes[bi.sys];
   double xp[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const size_t k = (size_t)c * s.npad + p;
-    xp[c] = s.x[k] + dt * s.v[k] + dt * dt * s.f[k] / 2.;
+    xp[c] = drift_pos(box, s.x[k], s.v[k], s.f[k]);
   }
   s.q[p] = shadow_of(s.sc[bi.sys], xp[0], xp[1], xp[2]);
 }
 
-// Close of a fused TVN step (MDSystem.cpp:498-506 and :578-579): with chi of
-// the box computed by the pair kernel's last block, v = (2 chi - 1) v +
-// chi dt tF, boundaries, K, the next step's predictor, and -- in the last
-// CTA to finish -- the observables of every box.
+// Close of a fused TVN step (MDSystem.cpp:469-506, :578-579).  The pair
+// kernel's epilogue left F_{n+1} in s.tf (s.f still holds F_n), e and w, and
+// chi of every box.  Per particle: x_{n+1} = drift_pos(x_n, v_n, F_n),
+// tF = F_n/2 + F_{n+1}/2, v = (2 chi - 1) v + chi dt tF, boundaries,
+// F <- F_{n+1}, the next step's predictor, and block partials K, V, W; the
+// last CTA to finish computes the observables of every box.
 __global__ void k_tvn_close(StateArgs s) {
   __shared__ double sh[3 * 32];
   __shared__ int last;
@@ -354,17 +352,20 @@ __global__ void k_tvn_close(StateArgs s) {
   const BoxArgs box = s.boxes[bi.sys];
   const DevScalars& sc = s.sc[bi.sys];
   const double chi = sc.chi;
-  const double dt = box.dt;
-  double part[1] = {0.0};
+  const double a1 = 2. * chi - 1., b1 = chi * box.dt;
+  double part[3] = {0.0, 0.0, 0.0};
   if (tid < bi.n_i) {
     const int p = bi.p0 + bi.i0 + tid;
-    double x[3], v[3], f[3];
+    double x[3], v[3], f1[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t k = (size_t)c * s.npad + p;
-      v[c] = (2. * chi - 1.) * s.v[k] + chi * dt * s.tf[k];
-      x[c] = s.x[k];
-      f[c] = s.f[k];
+      const double fn = s.f[k];
+      f1[c] = s.tf[k];
+      const double tf = 0.5 * fn + 0.5 * f1[c];
+      const double v0 = s.v[k];
+      x[c] = drift_pos(box, s.x[k], v0, fn);
+      v[c] = fma(a1, v0, b1 * tf);
     }
     apply_bc(box.bc, box.L, x, v);
     double xp[3];
@@ -373,14 +374,18 @@ __global__ void k_tvn_close(StateArgs s) {
       const size_t k = (size_t)c * s.npad + p;
       s.v[k] = v[c];
       s.x[k] = x[c];
-      xp[c] = x[c] + dt * v[c] + dt * dt * f[c] / 2.;
+      s.f[k] = f1[c];
+      xp[c] = drift_pos(box, x[c], v[c], f1[c]);
     }
     s.q_next[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
-    part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    part[0] = 0.5 * fma(v[0], v[0], fma(v[1], v[1], v[2] * v[2]));
+    part[1] = 0.5 * s.e[p];
+    part[2] = s.w[p];
   }
-  block_sum<1>(part, sh);
+  block_sum<3>(part, sh);
   if (tid == 0) {
-    s.blk_part[(size_t)B * 8 + 0] = part[0];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
     __threadfence();
     last = (atomicAdd(s.glob_cnt + 1, 1) == s.nblocks - 1);
   }

@@ -64,6 +64,16 @@ struct BoxArgs {
   double L, invL;
   double eps, sigma;
   double dt, T0, rho;
+  // Derived on the host from the fields above before every upload, so that
+  // the step kernels multiply instead of divide (FP64 division is a long
+  // dependent sequence on this part's narrow FP64 pipe).
+  double hdt;    // dt / 2
+  double hdt2;   // dt^2 / 2
+  double eps4;   // 4 eps
+  double kT;     // 2 / (3 N):  T = kT K
+  double kP;     // rho / N:    P = (W / 6 + N T) kP
+  double inv3N;  // 1 / (3 N):  Tkin = inv3N sum tv^2
+  double invT0;  // 1 / T0 (0 when T0 = 0)
 };
 
 }  // namespace ljgb

@@ -11,21 +11,38 @@
 
 namespace ljgb {
 
-// ApplyBoundaryConditions for one particle (MDSystem.cpp:406-436).
-__device__ __forceinline__ void apply_bc(int bc, double L, double (&x)[3], double (&v)[3]) {
+// ApplyBoundaryConditions (MDSystem.cpp:406-436) for one coordinate: wrap
+// (periodic) or reflect the velocity (walls); open boxes leave both alone.
+__device__ __forceinline__ void apply_bc1(int bc, double L, double& x, double& v) {
   if (bc == 0) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (x[c] < 0.) x[c] += L;
-      if (x[c] > L) x[c] -= L;
-    }
+    if (x < 0.) x += L;
+    if (x > L) x -= L;
   } else if (bc == 1) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (x[c] < 0. && v[c] < 0) v[c] = -v[c];
-      if (x[c] > L && v[c] > 0) v[c] = -v[c];
-    }
+    if (x < 0. && v < 0) v = -v;
+    if (x > L && v > 0) v = -v;
   }
+}
+
+// ApplyBoundaryConditions for one particle.
+__device__ __forceinline__ void apply_bc(int bc, double L, double (&x)[3], double (&v)[3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) apply_bc1(bc, L, x[c], v[c]);
+}
+
+// x + dt v + dt^2 F / 2: the drift of MDSystem.cpp:445 / :472, and the
+// predictor of the next step's positions.  Every kernel that drifts or
+// predicts calls this one form, so a prediction and the drift it stands for
+// agree bit for bit.
+__device__ __forceinline__ double drift_pos(const BoxArgs& b, double x, double v, double f) {
+  return fma(b.hdt2, f, fma(b.dt, v, x));
+}
+
+// chi = sqrt(T0 / Tkin) with Tkin = sum tv^2 / (3 N) (MDSystem.cpp:498-499),
+// as rsqrt(Tkin / T0): no FP64 division on the step's critical path.
+__device__ __forceinline__ double tvn_chi(const BoxArgs& b, double tv2, double* Tkin_out) {
+  const double Tkin = tv2 * b.inv3N;
+  *Tkin_out = Tkin;
+  return b.T0 > 0 ? rsqrt(Tkin * b.invT0) : sqrt(b.T0 / Tkin);
 }
 
 __device__ __forceinline__ int4 shadow_of(const DevScalars& sc, double x, double y, double z) {
@@ -71,8 +88,8 @@ __device__ __forceinline__ void observables_box(const StateArgs& s, int sys, dou
   if (threadIdx.x != 0) return;
   DevScalars& sc = s.sc[sys];
   const double N = (double)box.N;
-  const double T = 2. * K / 3. / N;
-  const double P = (W / 6. + N * T) / (N / box.rho);
+  const double T = K * box.kT;                           // 2 K / 3 / N
+  const double P = fma(W, 1. / 6., N * T) * box.kP;      // (W / 6 + N T) / (N / rho)
   const double U = K + V;
   sc.K = K;
   sc.V = V;
@@ -117,9 +134,10 @@ __device__ __forceinline__ void tvn_chi_box(const StateArgs& s, int sys, double*
   const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
   const double tv2 = box_sum(s, b0, b1, 3, sh);
   if (threadIdx.x == 0) {
-    const double Tkin = tv2 * (1. / 3. / box.N);
+    double Tkin;
+    const double chi = tvn_chi(box, tv2, &Tkin);
     s.sc[sys].Tkin = Tkin;
-    s.sc[sys].chi = sqrt(box.T0 / Tkin);
+    s.sc[sys].chi = chi;
   }
 }
 
@@ -144,80 +162,84 @@ __device__ __forceinline__ void segment_sums(const StateArgs& s, const BlockInfo
 // Fused second half of a step for block B, run by the CTA that wrote the last
 // pair-kernel segment of the block (blockDim.x = the i-block length).
 // Starts from the state at the beginning of the step (x_n, v_n, F_n); the
-// forces of this step were computed at x_{n+1} = x_n + dt v_n + dt^2 F_n / 2,
-// the predictor written by the previous step, recomputed here bit for bit.
-//   EVN (MDSystem.cpp:443-463): v_{n+1} = v_n + dt F_n/2 + dt F_{n+1}/2,
-//       boundaries, K, and the predictor of the next step into q_next.
-//   TVN (MDSystem.cpp:469-497): tF = F_n/2 + F_{n+1}/2, the half-kicked
-//       velocity's sum of squares (slot 3); v and the boundaries follow in
-//       k_tvn_close once chi is known.
-// Block partials: [0] K (EVN), [1] V, [2] W, [3] sum tv^2 (TVN).
+// forces of this step were computed at x_{n+1} = drift_pos(x_n, v_n, F_n),
+// the predictor written by the previous step.
+//   EVN (MDSystem.cpp:443-463): x_{n+1}; v_{n+1} = v_n + dt F_n/2 +
+//       dt F_{n+1}/2; boundaries; the predictor of the next step into
+//       q_next.  Block partials [0] K, [1] V, [2] W.
+//   TVN (MDSystem.cpp:469-497): only what chi needs before any velocity can
+//       be set -- F_{n+1} (kept in s.tf until k_tvn_close moves it to s.f),
+//       e, w, and the half-kicked velocity's sum of squares in partial [3].
+//       The drift, rescale, boundaries and predictor follow in k_tvn_close,
+//       which runs on every SM at once.
+// This code runs on whichever CTA finishes a block last, often several
+// blocks on one SM at the end of the pair kernel, and FP64 runs at 1/64 of
+// the FP32 rate here: the FP64 instruction count is kept to the minimum.
+// Not inlined: compiled into the pair kernel's loop body, its register needs
+// changed the allocation of the pair loop and cost 8% of the kernel's time
+// (A/B on GB300, N=16384); as a call it leaves the loop as it is.
 template <int MODE>
-__device__ __forceinline__ void fused_block_step(const StateArgs& s, int B, double* sh) {
+__device__ __noinline__ void fused_block_step(const StateArgs& s, int B, double* sh) {
   const BlockInfo bi = s.blocks[B];
   const int tid = threadIdx.x;
   const bool valid = tid < bi.n_i;
   const int p = bi.p0 + bi.i0 + tid;
   const BoxArgs box = s.boxes[bi.sys];
   const DevScalars& sc = s.sc[bi.sys];
-  const double dt = box.dt;
-  double part[4] = {0., 0., 0., 0.};
+  constexpr int NP = MODE == MODE_EVN ? 3 : 1;
+  double part[NP];
+#pragma unroll
+  for (int c = 0; c < NP; ++c) part[c] = 0.0;
   if (valid) {
     double S[5];
     segment_sums(s, bi, tid, S);
     const double fs = sc.fscale;
     const double Fn1[3] = {fs * S[0], fs * S[1], fs * S[2]};
-    const double e = 4.0 * box.eps * (S[3] - S[4]);
-    const double w = 4.0 * box.eps * (12.0 * S[3] - 6.0 * S[4]);
+    const double e = box.eps4 * (S[3] - S[4]);
+    const double w = box.eps4 * fma(12.0, S[3], -6.0 * S[4]);
     s.e[p] = e;
     s.w[p] = w;
-    part[1] = 0.5 * e;
-    part[2] = w;
-    double x[3], v[3], Fn[3];
+    if constexpr (MODE == MODE_EVN) {
+      double xp[3], vv = 0.0;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const size_t k = (size_t)c * s.npad + p;
-      x[c] = s.x[k];
-      v[c] = s.v[k];
-      Fn[c] = s.f[k];
-      x[c] += dt * v[c] + dt * dt * Fn[c] / 2.;
-      s.f[k] = Fn1[c];
-    }
-    if (MODE == MODE_EVN) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        v[c] += dt * Fn[c] / 2.;
-        v[c] += dt * Fn1[c] / 2.;
-      }
-      apply_bc(box.bc, box.L, x, v);
-      double xp[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
+      for (int c = 0; c < 3; ++c) {  // one component at a time: few live FP64 registers
         const size_t k = (size_t)c * s.npad + p;
-        s.x[k] = x[c];
-        s.v[k] = v[c];
-        xp[c] = x[c] + dt * v[c] + dt * dt * Fn1[c] / 2.;
+        const double Fn = s.f[k];
+        double v = s.v[k];
+        double x = drift_pos(box, s.x[k], v, Fn);
+        v = fma(box.hdt, Fn1[c], fma(box.hdt, Fn, v));
+        apply_bc1(box.bc, box.L, x, v);
+        s.f[k] = Fn1[c];
+        s.x[k] = x;
+        s.v[k] = v;
+        xp[c] = drift_pos(box, x, v, Fn1[c]);
+        vv = fma(v, v, vv);
       }
       s.q_next[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
-      part[0] = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      part[0] = 0.5 * vv;
+      part[1] = 0.5 * e;
+      part[2] = w;
     } else {
       double tv2 = 0.0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const size_t k = (size_t)c * s.npad + p;
-        s.x[k] = x[c];
-        const double tf = 0.5 * Fn[c] + 0.5 * Fn1[c];
-        s.tf[k] = tf;
-        const double tv = v[c] + dt * tf / 2.;
-        tv2 += tv * tv;
+        const double tf = 0.5 * s.f[k] + 0.5 * Fn1[c];  // as k_tvn_close forms it
+        s.tf[k] = Fn1[c];
+        const double tv = fma(box.hdt, tf, s.v[k]);
+        tv2 = fma(tv, tv, tv2);
       }
-      part[3] = tv2;
+      part[0] = tv2;
     }
   }
-  block_sum<4>(part, sh);
+  block_sum<NP>(part, sh);
   if (tid == 0) {
+    if constexpr (MODE == MODE_EVN) {
 #pragma unroll
-    for (int c = 0; c < 4; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
+      for (int c = 0; c < NP; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
+    } else {
+      s.blk_part[(size_t)B * 8 + 3] = part[0];
+    }
   }
 }
 

@@ -227,7 +227,16 @@ BoxArgs box_args(const lj_config& c) {
 
 lj_status upload_boxes(lj_system* s) {
   s->any_nonperiodic = false;
-  for (auto& b : s->boxes) s->any_nonperiodic |= (b.bc != 0);
+  for (auto& b : s->boxes) {
+    s->any_nonperiodic |= (b.bc != 0);
+    b.hdt = 0.5 * b.dt;
+    b.hdt2 = 0.5 * b.dt * b.dt;
+    b.eps4 = 4.0 * b.eps;
+    b.kT = 2.0 / (3.0 * b.N);
+    b.kP = b.rho / b.N;
+    b.inv3N = 1.0 / (3.0 * b.N);
+    b.invT0 = b.T0 > 0 ? 1.0 / b.T0 : 0.0;
+  }
   LJ_CUDA(s, cudaMemcpyAsync(s->dboxes.p, s->boxes.data(), sizeof(BoxArgs) * s->nsys, cudaMemcpyHostToDevice,
                              s->stream));
   return LJ_OK;
