@@ -267,6 +267,39 @@ lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_
 lj_status lj_forces_static(const float* pos4, float* force4, double* sums, int32_t n, float box,
                            int32_t periodic, void* stream);
 
+/* ---- Differentiable MD (adjoint) ----------------------------------------
+ * No counterpart in the reference (its dynamics are not differentiable).
+ * Gradients of a time-averaged trajectory loss
+ *   loss = (1/S) sum_{m=1..S} [ wK K_m/N + wV V_m/N + wP P_m ]
+ * over S EVN velocity-Verlet steps (MDSystem.cpp:443-463) of a periodic box,
+ * with respect to eps, sigma and the initial positions and velocities, by a
+ * discrete adjoint: FP64 forward pass keeping (x, v, F) every
+ * `checkpoint_every` steps, then a reverse sweep that replays each segment
+ * from its checkpoint and applies the force Jacobian-vector product
+ * (Hessian . vector) on the GPU.  Everything runs in FP64; the gradients are
+ * those of this forward pass (the same equations as lj_step with
+ * LJ_PREC_FP64, summed in a different order). */
+typedef struct lj_adjoint lj_adjoint;
+
+/* cfg: n, density, temperature, epsilon, sigma, lattice, jitter, seed and
+ * device as for lj_create (the initial state is sampled the same way);
+ * boundary must be LJ_BC_PERIODIC and canonical 0 (LJ_ERR_UNSUPPORTED
+ * otherwise: wall reflections and the TVN rescale are not differentiated).
+ * Default loss weights: wK = 0, wV = 1, wP = 1. */
+lj_status lj_adjoint_create(const lj_config* cfg, int32_t checkpoint_every, lj_adjoint** out);
+lj_status lj_adjoint_destroy(lj_adjoint* adj);
+const char* lj_adjoint_last_error(const lj_adjoint* adj);
+/* Initial state (N x 3 each, interleaved). */
+lj_status lj_adjoint_set_state(lj_adjoint* adj, const double* pos, const double* vel);
+lj_status lj_adjoint_set_loss(lj_adjoint* adj, double w_kinetic, double w_potential, double w_pressure);
+/* Runs nsteps steps of size dt from the initial state; writes the loss. */
+lj_status lj_adjoint_forward(lj_adjoint* adj, double dt, int32_t nsteps, double* loss);
+/* K, V, W after each step of the last forward pass (any may be NULL). */
+lj_status lj_adjoint_observables(lj_adjoint* adj, double* K, double* V, double* W, int32_t max, int32_t* count);
+/* dloss/deps, dloss/dsigma, dloss/dpos (N x 3), dloss/dvel (N x 3) of the last
+ * forward pass (any output may be NULL). */
+lj_status lj_adjoint_backward(lj_adjoint* adj, double* d_epsilon, double* d_sigma, double* d_pos, double* d_vel);
+
 /* Page-locked host memory for lj_set_state / lj_get_state buffers: copies
  * from and to it run as direct DMA.  NULL on failure; free with lj_host_free. */
 void* lj_host_alloc(size_t bytes);

@@ -117,6 +117,14 @@ def _declare(L):
                                     C.c_float, C.c_int, C.c_int]),
         "threadSync": (None, []),
         "threadExit": (None, []),
+        "lj_adjoint_create": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(_P)]),
+        "lj_adjoint_destroy": (C.c_int, [_P]),
+        "lj_adjoint_last_error": (C.c_char_p, [_P]),
+        "lj_adjoint_set_state": (C.c_int, [_P, _P, _P]),
+        "lj_adjoint_set_loss": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
+        "lj_adjoint_forward": (C.c_int, [_P, C.c_double, C.c_int32, _dp]),
+        "lj_adjoint_observables": (C.c_int, [_P, _P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]),
+        "lj_adjoint_backward": (C.c_int, [_P, _dp, _dp, _P, _P]),
         "lj_reference_abi_status": (C.c_int, []),
         "lj_reference_abi_error": (C.c_char_p, []),
     }
@@ -399,3 +407,63 @@ class System:
 
     def launch_count(self) -> int:
         return int(load().lj_kernel_launch_count(self.h))
+
+
+class Adjoint:
+    """Differentiable trajectory loss (lj_adjoint_*): FP64 forward pass with
+    checkpoints and the discrete adjoint (force Hessian-vector products on
+    the GPU).  loss = (1/S) sum_m [wK K_m/N + wV V_m/N + wP P_m]."""
+
+    def __init__(self, cfg: Optional[Config] = None, checkpoint_every: int = 20, **kw):
+        L = load()
+        cfg = cfg if cfg is not None else config(**kw)
+        h = _P()
+        code = L.lj_adjoint_create(C.byref(cfg), int(checkpoint_every), C.byref(h))
+        if code != LJ_OK:
+            raise LJError(code, "lj_adjoint_create failed")
+        self.h = h
+        self.cfg = cfg
+        self.n = cfg.n
+
+    def _c(self, code):
+        if code != LJ_OK:
+            msg = load().lj_adjoint_last_error(self.h)
+            raise LJError(code, msg.decode() if msg else "")
+
+    def set_state(self, pos, vel):
+        p = _f64(pos, 3 * self.n)
+        v = _f64(vel, 3 * self.n)
+        self._c(load().lj_adjoint_set_state(self.h, p.ctypes.data, v.ctypes.data))
+
+    def set_loss(self, w_kinetic=0.0, w_potential=1.0, w_pressure=1.0):
+        self._c(load().lj_adjoint_set_loss(self.h, w_kinetic, w_potential, w_pressure))
+
+    def forward(self, dt: float, nsteps: int) -> float:
+        out = C.c_double()
+        self._c(load().lj_adjoint_forward(self.h, dt, int(nsteps), C.byref(out)))
+        return out.value
+
+    def observables(self):
+        cnt = C.c_int32()
+        self._c(load().lj_adjoint_observables(self.h, None, None, None, 0, C.byref(cnt)))
+        K, V, W = (np.zeros(cnt.value) for _ in range(3))
+        self._c(load().lj_adjoint_observables(self.h, K.ctypes.data, V.ctypes.data, W.ctypes.data, cnt.value, None))
+        return dict(K=K, V=V, W=W)
+
+    def backward(self):
+        de, ds = C.c_double(), C.c_double()
+        dp = np.zeros((self.n, 3))
+        dv = np.zeros((self.n, 3))
+        self._c(load().lj_adjoint_backward(self.h, C.byref(de), C.byref(ds), dp.ctypes.data, dv.ctypes.data))
+        return de.value, ds.value, dp, dv
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lj_adjoint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -26,6 +26,7 @@ SOURCES = [
     "lj_integrate.cu",
     "lj_compat.cu",
     "lj_noalloc.cu",
+    "lj_adjoint.cu",
     "lj_system.cpp",
     "lj_schedule.cpp",
     "lj_init.cpp",
