@@ -1,0 +1,158 @@
+"""The benchmark configurations end to end (GPU tests).
+
+Each test runs one configuration of the path as specified -- sizes,
+densities, temperatures, lattices, ensembles, step counts -- through the C ABI
+and checks it against the FP64 oracle or the all-FP64 GPU path:
+
+  * plain method: N=400, rho*=0.05, T*=1.4, SC lattice +-0.05 sigma jitter,
+    Maxwell velocities, dt=0.005, EVN, 1000 steps, FP64; per-step K, V, W
+    against the FP64 oracle and a 200-bin RDF to r = L/2;
+  * dense liquid: N=16384, rho*=0.85, T*=1.0, FCC +-0.02, dt=0.005, TVN;
+    mixed precision step by step (first 10 steps) against the all-FP64 run,
+    then time averages of U/N and P against the all-FP64 run;
+  * large single system: N=262144, rho*=1.1 (solid), T*=1.0, FCC +-0.01,
+    dt=0.004, TVN; forces on a 4096-particle seeded subset against the FP64
+    oracle, then TVN steps;
+  * energy drift of the mixed path against the FP64 path over 1e5 EVN steps.
+"""
+import numpy as np
+import pytest
+
+import lj_testutil as U
+
+pytestmark = pytest.mark.gpu
+
+
+def _blocks_sem(x, nblocks=10):
+    """Standard error of the mean from block averages."""
+    b = np.array_split(np.asarray(x), nblocks)
+    m = np.array([blk.mean() for blk in b])
+    return m.std(ddof=1) / np.sqrt(len(m))
+
+
+def test_plain_method_configuration(ljgb_mod, oracle_mod):
+    N, rho, T0, dt, S = 400, 0.05, 1.4, 0.005, 1000
+    cfg = ljgb_mod.config(n=N, density=rho, temperature=T0, canonical=0, lattice=ljgb_mod.LATTICE_SC,
+                          jitter=0.05, seed=400, precision=ljgb_mod.PREC_FP64)
+    pos, vel = ljgb_mod.sample_initial_state(cfg)
+    assert np.abs(vel.sum(0)).max() < 1e-10                          # zero net momentum
+    assert 0.5 * (vel * vel).sum() * 2 / 3 / N == pytest.approx(T0, rel=1e-12)
+    s = ljgb_mod.System(cfg=cfg)
+    s.set_recording(S)
+    s.integrate(dt, S)
+    rec = s.records()
+    assert len(rec) == S and rec[-1]["step"] == S
+    o = oracle_mod.F64System(pos, vel, s.L, rho, T0, False, 0)
+    K, V, W = np.zeros(S), np.zeros(S), np.zeros(S)
+    for m in range(S):
+        o.step(dt)
+        K[m], V[m], W[m] = o.K, o.V, o.W
+    for key, ref in (("K", K), ("V", V), ("W", W)):
+        got = np.array([r[key] for r in rec])
+        err = np.abs(got - ref).max() / np.abs(ref).max()
+        print("plain method: per-step %s max rel deviation from the FP64 oracle over %d steps: %.2e" % (key, S, err))
+        assert err < 3e-9, key
+    # 200-bin RDF to r = L/2 of the final state (exact counts, device binning rule)
+    p, _, _ = s.get_state()
+    dr = (s.L / 2) / 200
+    got = s.rdf_counts(ljgb_mod.RDF_R_LINEAR, 200, dr)
+    ks = s.L / (4294967296.0 * 1.0)
+    want = oracle_mod.emu_rdf_r(oracle_mod.emu_fixed(p, s.L), np.float32(ks * ks), np.float32(1.0 / dr),
+                                np.float32((200 * dr) ** 2), 200)
+    assert np.array_equal(got, want)
+    # every pair closer than L/2 is counted once per ordered pair
+    d = p[:, None, :] - p[None, :, :]
+    d -= s.L * np.round(d / s.L)
+    r = np.sqrt((d * d).sum(-1))[~np.eye(N, dtype=bool)]
+    assert abs(int(got.sum()) - int((r < s.L / 2).sum())) <= 4
+
+
+def test_dense_liquid_configuration(ljgb_mod):
+    N, rho, T0, dt = 16384, 0.85, 1.0, 0.005
+    kw = dict(n=N, density=rho, temperature=T0, canonical=1, lattice=ljgb_mod.LATTICE_FCC, jitter=0.02, seed=2)
+    mixed = ljgb_mod.System(**kw, precision=ljgb_mod.PREC_MIXED)
+    fp64 = ljgb_mod.System(**kw, precision=ljgb_mod.PREC_FP64)
+    L = mixed.L
+    # step by step, first 10 steps
+    for k in range(10):
+        mixed.integrate(dt)
+        fp64.integrate(dt)
+        pm, vm, fm = mixed.get_state()
+        pd, vd, fd = fp64.get_state()
+        dp = pm - pd
+        dp -= L * np.round(dp / L)
+        om, od = mixed.observables(), fp64.observables()
+        err = U.force_errors(fm, fd)
+        print("dense liquid step %d: |dx| %.2e |dv| %.2e force gate %.2e dU/N %.2e dP %.2e" % (
+            k + 1, np.abs(dp).max(), np.abs(vm - vd).max(), err["gate_max"], abs(om["U"] - od["U"]) / N,
+            abs(om["P"] - od["P"])))
+        assert np.abs(dp).max() < 1e-6 * L
+        assert np.abs(vm - vd).max() < 1e-5
+        assert err["gate_max"] < 1e-5
+        assert om["T"] == pytest.approx(od["T"], rel=1e-7)
+        assert om["U"] == pytest.approx(od["U"], rel=1e-6)
+        assert om["P"] == pytest.approx(od["P"], rel=1e-5)
+    # averages: both runs continue; trajectories decorrelate, the averages
+    # must agree within their statistical errors
+    n_avg = 400
+    mixed.set_recording(n_avg)
+    fp64.set_recording(n_avg)
+    mixed.integrate(dt, n_avg)
+    fp64.integrate(dt, n_avg)
+    res = {}
+    for name, s in (("mixed", mixed), ("fp64", fp64)):
+        rec = s.records()
+        u = np.array([r["U"] for r in rec]) / N
+        p = np.array([r["P"] for r in rec])
+        res[name] = (u.mean(), _blocks_sem(u), p.mean(), _blocks_sem(p))
+    (um, su_m, pm_, sp_m), (ud, su_d, pd_, sp_d) = res["mixed"], res["fp64"]
+    print("dense liquid averages over %d steps: U/N %.8f (mixed) %.8f (fp64) +-%.1e; P %.7f / %.7f +-%.1e"
+          % (n_avg, um, ud, su_d, pm_, pd_, sp_d))
+    assert abs(um - ud) < 5 * np.hypot(su_m, su_d) + 1e-4
+    assert abs(pm_ - pd_) < 5 * np.hypot(sp_m, sp_d) + 1e-3
+
+
+def test_large_single_system_configuration(ljgb_mod, oracle_mod):
+    N, rho, T0, dt = 262144, 1.1, 1.0, 0.004
+    s = ljgb_mod.System(n=N, density=rho, temperature=T0, canonical=1, lattice=ljgb_mod.LATTICE_FCC, jitter=0.01,
+                        seed=262144)
+    pos, _, F = s.get_state()
+    i0 = int(np.random.default_rng(4096).integers(0, N - 4096))
+    r = oracle_mod.f64_forces(pos, s.L, True, rows=(i0, i0 + 4096))
+    err = U.force_errors(F[i0:i0 + 4096], r["F"])
+    print("large system: 4096 rows from %d vs FP64 oracle: %s" % (i0, err))
+    assert err["gate_max"] <= 1e-5 and err["rel_median"] <= 1e-5
+    e, _ = s.pair_sums()
+    assert np.abs(e[i0:i0 + 4096] - r["e"]).max() <= 1e-5 * np.abs(r["e"]).max()
+    s.integrate(dt, 20)
+    o = s.observables()
+    assert o["step"] == 20 and np.isfinite(o["U"])
+    # TVN: chi = sqrt(T0 / Tkin) of the half-kicked velocities keeps both near T0
+    assert o["Tkin_tvn"] == pytest.approx(T0, rel=0.02)
+    assert abs(o["T"] - T0) < 0.05
+
+
+def test_energy_drift_mixed_vs_fp64(ljgb_mod):
+    """EVN, N=2048, rho*=0.85, T*=1.0, dt=0.005, 1e5 steps: the drift of the
+    total energy per particle of the mixed path against the all-FP64 path."""
+    N, rho, dt, S, every = 2048, 0.85, 0.005, 100000, 1000
+    kw = dict(n=N, density=rho, temperature=1.0, canonical=0, lattice=ljgb_mod.LATTICE_FCC, jitter=0.02, seed=5)
+    fit = {}
+    for name, prec in (("mixed", ljgb_mod.PREC_MIXED), ("fp64", ljgb_mod.PREC_FP64)):
+        s = ljgb_mod.System(**kw, precision=prec)
+        s.integrate(dt, 2000)                      # equilibrate from the lattice
+        u = []
+        for _ in range(S // every):
+            s.integrate(dt, every)
+            u.append(s.observables()["U"] / N)
+        u = np.array(u)
+        t = dt * every * np.arange(1, len(u) + 1)
+        slope, icpt = np.polyfit(t, u, 1)
+        resid = u - (slope * t + icpt)
+        fit[name] = (slope, resid.std(), u.max() - u.min())
+        print("energy drift %s: dU/N/dt %.3e per tau, residual %.2e, range %.2e over %d steps" % (
+            name, slope, resid.std(), u.max() - u.min(), S))
+    (sm, rm, _), (sd, rd, _) = fit["mixed"], fit["fp64"]
+    T = dt * S
+    # difference of the drifts over the whole run, against the fluctuation level
+    assert abs(sm - sd) * T < 5 * max(rm, rd) + 1e-5
