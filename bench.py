@@ -18,7 +18,12 @@ Prints one JSON line (rank 0):
   accuracy    per-particle force error of the mixed path vs FP64;
   roofline    pair kernel vs the FP32 peak (38 flops per ordered pair);
   cpu_baseline the reference's CPU algorithm (float-storage restatement of
-              MDSystem.cpp's CPU path) on the host cores, a bounded sample.
+              MDSystem.cpp's CPU path) on the host cores, a bounded sample;
+  configs     the other configurations, measured briefly on the same GPU:
+              256 batched replicas (aggregate steps/s and pair-interactions/s),
+              N = 262144 (pair-interactions/s, FP32 fraction, subset force
+              error vs the FP64 oracle) and the adjoint at N = 2048 (forward
+              and backward time of 200 steps).
 
 --impl reference times that CPU implementation alone on the same workload.
 Multi-GPU (torchrun): every rank runs an independent replica (the path has
@@ -48,7 +53,7 @@ T0 = 1.0
 DT = 0.005
 JITTER = 0.02
 SEED = 2
-FLOPS_PER_PAIR = 38  # FMA = 2, rcp = 1 (roofline numerator)
+FLOPS_PER_PAIR = 38  # algorithmic FP32 flops per ordered pair, FMA = 2, rcp = 1
 WORKLOAD = "lj-dense-liquid-tvn N=16384 rho*=0.85 T*=1.0 FCC+0.02 dt=0.005"
 
 
@@ -156,14 +161,14 @@ def make_system(ljgb, prec, device):
                        seed=SEED, precision=prec, device=device)
 
 
-def timed_steps(torch, s, steps, warmup, flush):
+def timed_steps(torch, s, steps, warmup, flush, dt=DT):
     """Per-step CUDA-event timing on the library's stream, L2 flushed before
     every timed step (flush writes a buffer larger than L2)."""
     ext = torch.cuda.ExternalStream(s.stream())
     for _ in range(warmup):
         with torch.cuda.stream(ext):
             flush.zero_()
-        s.integrate(DT)
+        s.integrate(dt)
     s.sync()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
@@ -172,7 +177,7 @@ def timed_steps(torch, s, steps, warmup, flush):
         with torch.cuda.stream(ext):
             flush.zero_()
             starts[k].record(ext)
-        s.integrate(DT)
+        s.integrate(dt)
         with torch.cuda.stream(ext):
             ends[k].record(ext)
     s.sync()
@@ -262,6 +267,74 @@ def accuracy(ljgb, oracle, device):
     return out
 
 
+def batch_configs(ljgb, seed=3, k=256):
+    """The batched-replicas configuration: 256 boxes, N in [200, 4000),
+    rho* in [0.01, 1.1], T* in [0.7, 2.0], half periodic and half hard-wall,
+    FCC + 0.02 jitter, TVN."""
+    rng = np.random.default_rng(seed)
+    return [ljgb.config(n=int(rng.integers(200, 4000)), density=float(rng.uniform(0.01, 1.1)),
+                        temperature=float(rng.uniform(0.7, 2.0)), canonical=1, boundary=i % 2,
+                        lattice=ljgb.LATTICE_FCC, jitter=0.02, seed=1000 + i) for i in range(k)]
+
+
+def extra_configs(torch, ljgb, oracle, dev, flush, peak):
+    """Short measurements of the other configurations (rank 0)."""
+    out = {}
+    # 256 batched replicas, dt = 0.004, TVN, one persistent pair launch per step
+    cfgs = batch_configs(ljgb)
+    b = ljgb.System(batch=cfgs)
+    b.autotune()
+    steps = 20
+    ms, _, launches = timed_steps(torch, b, steps, 3, flush, dt=0.004)
+    pairs = float(sum(c.n * (c.n - 1) for c in cfgs))
+    out["batch_256"] = {
+        "workload": "256 replicas, N U[200,4000) (sum %d), rho* U[0.01,1.1], T* U[0.7,2.0], half walls, TVN, "
+                    "dt=0.004" % sum(c.n for c in cfgs),
+        "ms_per_step": ms / steps, "steps_per_s": 1e3 * steps / ms, "replica_steps_per_s": 256e3 * steps / ms,
+        "pair_interactions_per_s": pairs * steps / (ms * 1e-3), "gpu_launches_per_step": launches / steps,
+        "l2": "flushed before every timed step"}
+    b.close()
+    # one large box: N = 262144, rho* = 1.1, T* = 1.0, FCC + 0.01, dt = 0.004, TVN
+    n = 262144
+    g = ljgb.System(n=n, density=1.1, temperature=1.0, canonical=1, lattice=ljgb.LATTICE_FCC, jitter=0.01,
+                    seed=262144, device=dev, autotune=0)
+    pos, _, F = g.get_state()
+    i0 = int(np.random.default_rng(4096).integers(0, n - 4096))
+    r = oracle.f64_forces(pos, g.L, True, rows=(i0, i0 + 4096))
+    d = np.linalg.norm(F[i0:i0 + 4096] - r["F"], axis=1)
+    mag = np.linalg.norm(r["F"], axis=1)
+    rms = float(np.sqrt(np.mean(mag ** 2)))
+    steps = 5
+    ms, _, _ = timed_steps(torch, g, steps, 2, flush, dt=0.004)
+    g.profile(True)
+    g.integrate(0.004, steps)
+    prof = g.profile_read()
+    g.profile(False)
+    pair_ms = prof["pair_ms"] / max(1, prof["pair_launches"])
+    g.close()
+    out["large_262144"] = {
+        "workload": "N=262144 rho*=1.1 T*=1.0 FCC+0.01 dt=0.004 TVN", "ms_per_step": ms / steps,
+        "pair_interactions_per_s": n * (n - 1) * steps / (ms * 1e-3), "pair_kernel_ms": pair_ms,
+        "fp32_frac": FLOPS_PER_PAIR * n * (n - 1) / (pair_ms * 1e-3) / 1e12 / peak,
+        "subset_vs_fp64_oracle": {"rows": [i0, i0 + 4096], "gate_max": float((d / np.maximum(mag, rms)).max()),
+                                  "rel_median": float(np.median(d / mag))}}
+    # adjoint: N = 2048, rho* = 0.85, 200 EVN steps, checkpoints every 20, FP64
+    a = ljgb.Adjoint(n=2048, density=0.85, temperature=1.0, lattice=ljgb.LATTICE_FCC, jitter=0.02, seed=2048,
+                     checkpoint_every=20)
+    a.forward(0.005, 200)
+    a.backward()
+    t0 = time.perf_counter()
+    a.forward(0.005, 200)
+    t1 = time.perf_counter()
+    a.backward()
+    t2 = time.perf_counter()
+    a.close()
+    out["adjoint_2048"] = {"workload": "N=2048 rho*=0.85 T*=1.0 dt=0.005, 200 EVN steps, checkpoints every 20, "
+                                       "loss <V/N + P>, FP64", "forward_ms": (t1 - t0) * 1e3,
+                           "backward_ms": (t2 - t1) * 1e3, "timing": "host wall clock, synchronised"}
+    return out
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import ljgb
@@ -322,6 +395,7 @@ def gpu_arm(args, rank, world, local_rank):
         achieved = FLOPS_PER_PAIR * pairs_step / (pair_ms * 1e-3) / 1e12
         traffic = read_traffic()
         cpu = cpu_baseline(max_seconds=args.cpu_seconds)
+        extra = extra_configs(torch, ljgb, oracle, dev, flush, peak) if not args.no_extra else None
         result = {
             "metric": "pair-interactions/s, N=16384, FP32-mixed vs FP64 same GB300 @ force rel err<=1e-5",
             "value": value, "unit": "pair-interactions/s", "n_gpus": world, "steps": args.steps,
@@ -339,7 +413,7 @@ def gpu_arm(args, rank, world, local_rank):
             "accuracy": acc,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_pairs_mixed", "flops_per_pair": FLOPS_PER_PAIR,
+                         "kernel": "k_pairs_mixed_fused", "flops_per_pair": FLOPS_PER_PAIR,
                          "pair_kernel_ms": pair_ms, "step_ms_profiled": step_ms_prof,
                          "step_frac": FLOPS_PER_PAIR * pairs_step / (ms_step * 1e-3) / 1e12 / peak,
                          "peak_source": "nominal FP32: %d SMs x 128 lanes x 2 x %.0f MHz (MEASURED_PEAKS.json "
@@ -348,6 +422,8 @@ def gpu_arm(args, rank, world, local_rank):
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }
+        if extra:
+            result["configs"] = extra
     return result
 
 
@@ -397,6 +473,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
