@@ -282,6 +282,7 @@ __global__ void k_tvn_finish(StateArgs s) {
     chi_sh = chi;
     if (B == b0) {
       s.sc[bi.sys].Tkin = Tkin;
+      s.sc[bi.sys].Tkin_rec = Tkin;
       s.sc[bi.sys].chi = chi;
     }
   }
@@ -338,11 +339,14 @@ __global__ void k_predict(StateArgs s) {
 // kernel's epilogue left F_{n+1} in s.tf (s.f still holds F_n), e and w, and
 // chi of every box.  Per particle: x_{n+1} = drift_pos(x_n, v_n, F_n),
 // tF = F_n/2 + F_{n+1}/2, v = (2 chi - 1) v + chi dt tF, boundaries,
-// F <- F_{n+1}, the next step's predictor, and block partials K, V, W; the
-// last CTA to finish computes the observables of every box.
+// F <- F_{n+1}, the next step's predictor, and block partials K, V, W.
+// The observables of the step (sums over blocks, averages, record) are left
+// pending: the next step's pair kernel computes them in a CTA that has
+// finished its pair work (pending_observables), or k_obs_finalize does
+// before the host reads them.  This takes a serial last-CTA stage off the
+// step's critical path.
 __global__ void k_tvn_close(StateArgs s) {
   __shared__ double sh[3 * 32];
-  __shared__ int last;
   // Launched as a programmatic dependent of the pair kernel: the CTAs start
   // while the pair grid drains and wait here until its writes are visible.
   asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -350,7 +354,7 @@ __global__ void k_tvn_close(StateArgs s) {
   const BlockInfo bi = s.blocks[B];
   const int tid = threadIdx.x;
   const BoxArgs box = s.boxes[bi.sys];
-  const DevScalars& sc = s.sc[bi.sys];
+  DevScalars& sc = s.sc[bi.sys];
   const double chi = sc.chi;
   const double a1 = 2. * chi - 1., b1 = chi * box.dt;
   double part[3] = {0.0, 0.0, 0.0};
@@ -386,15 +390,18 @@ __global__ void k_tvn_close(StateArgs s) {
   if (tid == 0) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
-    __threadfence();
-    last = (atomicAdd(s.glob_cnt + 1, 1) == s.nblocks - 1);
+    if (B == s.sys_block_first[bi.sys]) {
+      sc.Tkin_rec = sc.Tkin;
+      sc.obs_pending = 1;
+    }
+    if (B == 0) s.glob_cnt[1] = 0;  // ticket counter of the next pair kernel's pending_observables
   }
-  __syncthreads();
-  if (last) {
-    __threadfence();
-    for (int sys = 0; sys < s.nsys; ++sys) observables_box<MODE_TVN>(s, sys, sh);
-    if (tid == 0) s.glob_cnt[1] = 0;
-  }
+}
+
+// Observables left pending by the last fused TVN step (one CTA per box).
+__global__ void k_obs_finalize(StateArgs s) {
+  __shared__ double sh[3 * 32];
+  pending_observables(s, blockIdx.x, gridDim.x, sh);
 }
 
 // |v| histogram (MDSystem.cpp:658-662): b = floor(sqrt(v.v)/step), b < nb.
@@ -518,6 +525,11 @@ cudaError_t launch_observables(const StateArgs& s, int nsys, int mode, cudaStrea
 
 cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t st) {
   k_predict<<<nblocks, bi, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_obs_finalize(const StateArgs& s, int nsys, cudaStream_t st) {
+  k_obs_finalize<<<nsys, kObsThreads, 0, st>>>(s);
   return cudaGetLastError();
 }
 

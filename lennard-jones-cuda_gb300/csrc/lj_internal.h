@@ -33,6 +33,13 @@ struct DevScalars {
   int status;
   int rec_cap;
   long long rec_count;
+  // Fused TVN steps compute a step's observables late (inside the next
+  // step's pair kernel, or in k_obs_finalize): obs_pending marks a box whose
+  // K/V/W block partials are written but not yet summed; Tkin_rec is the
+  // Tkin of that step for its record.
+  double Tkin_rec;
+  int obs_pending;
+  int pad_;
 };
 
 // Observable record layout written by the device (matches lj_observables).

@@ -85,7 +85,7 @@ struct StateArgs {
   int* status;
   int4* q_next;                // fused step: predictor shadow for the next step
   int* blk_cnt;                // fused step: segments finished per i-block
-  int* glob_cnt;               // fused step: blocks finished (2 counters)
+  int* glob_cnt;               // fused step: [0] blocks finished, [1] pending-observables tickets
   int nblocks;                 // i-blocks of all boxes
   int nsys;                    // boxes
 };
@@ -110,6 +110,7 @@ cudaError_t launch_velocity_hist(const StateArgs& s, int nblocks, int bi, double
                                  unsigned long long* counts, cudaStream_t st);
 cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
 cudaError_t launch_tvn_close(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
+cudaError_t launch_obs_finalize(const StateArgs& s, int nsys, cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,

@@ -339,9 +339,19 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     }
   }
 
-  // The dependent kernel of a fused TVN step (k_tvn_close) may be scheduled
-  // from here on; it waits for this grid's completion before reading.
-  if (EPI == MODE_TVN) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (EPI == MODE_TVN) {
+    // This CTA's pair work is done: the first CTAs to get here compute the
+    // observables the previous step's k_tvn_close left pending (one box per
+    // ticket), in time the SM would otherwise leave to the CTAs still busy.
+    __shared__ int ticket;
+    __syncthreads();
+    if (tid == 0) ticket = atomicAdd(st.glob_cnt + 1, 1);
+    __syncthreads();
+    if (ticket < st.nsys && !sfail) pending_observables(st, ticket, gridDim.x, shd);
+    // The dependent kernel of a fused TVN step (k_tvn_close) may be scheduled
+    // from here on; it waits for this grid's completion before reading.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  }
   __syncthreads();
   if (sfail) {
     // Drain the copies still in flight before the CTA's shared memory goes away.

@@ -117,13 +117,29 @@ __device__ __forceinline__ void observables_box(const StateArgs& s, int sys, dou
     r.U = U;
     r.W = W;
     r.Pshear = sc.Pshear;
-    r.Tkin = sc.Tkin;
+    r.Tkin = MODE == MODE_TVN ? sc.Tkin_rec : sc.Tkin;
     r.av_U = sc.av_U;
     r.av_T = sc.av_T;
     r.av_p = sc.av_p;
     r.av_iters = sc.av_iters;
     r.step = sc.step;
     sc.rec_count += 1;
+  }
+}
+
+// Observables of the boxes whose fused TVN step left them pending (block
+// partials K, V, W written by k_tvn_close).  Called with a ticket from
+// 0 .. tickets-1; ticket k takes boxes k, k + tickets, ...  Block-wide call.
+static __device__ __noinline__ void pending_observables(const StateArgs& s, int ticket, int tickets, double* sh) {
+  __shared__ int pend;
+  for (int sys = ticket; sys < s.nsys; sys += tickets) {
+    if (threadIdx.x == 0) pend = s.sc[sys].obs_pending;
+    __syncthreads();
+    if (pend) {
+      observables_box<MODE_TVN>(s, sys, sh);
+      if (threadIdx.x == 0) s.sc[sys].obs_pending = 0;
+    }
+    __syncthreads();
   }
 }
 

@@ -83,6 +83,7 @@ struct lj_system {
   DevBuf<double4_32a> xd;
   DevBuf<int> blk_cnt, glob_cnt;  // fused-step completion counters
   int qpar = 0;             // which of q / q2 holds the current shadow
+  bool obs_maybe_pending = false;  // a fused TVN step left observables pending (DevScalars::obs_pending)
   bool pred_ready = false;  // current shadow = predictor x + dt v + dt^2 F/2 for pred_dt
   double pred_dt = 0.0;
   DevBuf<BlockInfo> blocks;
@@ -133,6 +134,8 @@ lj_status fail(lj_system* s, lj_status code, const char* fmt, ...) {
       return fail(sys, e_ == cudaErrorMemoryAllocation ? LJ_ERR_OUT_OF_MEMORY : LJ_ERR_CUDA,    \
                   "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
   } while (0)
+
+lj_status flush_observables(lj_system* s);
 
 StateArgs state_args(lj_system* s) {
   StateArgs a{};
@@ -318,7 +321,9 @@ lj_status enqueue_pairs(lj_system* s, bool forces, bool hist, const HistArgs* h)
 // Force evaluation + observables at the current positions (CalculateForces +
 // CalculateParameters).
 lj_status enqueue_compute_forces(lj_system* s) {
-  lj_status st = enqueue_frame_all(s);
+  lj_status st = flush_observables(s);
+  if (st) return st;
+  st = enqueue_frame_all(s);
   if (st) return st;
   st = enqueue_pairs(s, true, false, nullptr);
   if (st) return st;
@@ -341,6 +346,10 @@ cudaEvent_t next_event(lj_system* s) {
 // The kernels of one Verlet step, enqueued on s->stream (captured or not).
 // ev (optional): events recorded at step start, pair start, pair end, step end.
 lj_status enqueue_step(lj_system* s, int mode, cudaEvent_t* ev, bool capture, int* kernels) {
+  if (!capture) {
+    lj_status st = flush_observables(s);
+    if (st) return st;
+  }
   StateArgs a = state_args(s);
   const int nb = nblocks(s);
   int k = 0;
@@ -458,7 +467,21 @@ lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
   return LJ_OK;
 }
 
+// Computes the observables that fused TVN steps left pending
+// (k_obs_finalize; boxes whose observables a later pair kernel already
+// computed are skipped on the device).  Called before anything reads or
+// changes the observables, the running sums or the block partials.
+lj_status flush_observables(lj_system* s) {
+  if (!s->obs_maybe_pending) return LJ_OK;
+  s->obs_maybe_pending = false;
+  LJ_CUDA(s, launch_obs_finalize(state_args(s), s->nsys, s->stream));
+  s->launches += 1;
+  return LJ_OK;
+}
+
 lj_status check_status(lj_system* s) {
+  lj_status fst = flush_observables(s);
+  if (fst) return fst;
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   int st = 0;
   LJ_CUDA(s, cudaMemcpy(&st, s->status.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -527,6 +550,8 @@ lj_status download_xyz(lj_system* s, const double* dev, double* host) {
 }
 
 lj_status read_scalars(lj_system* s, std::vector<DevScalars>& out) {
+  lj_status st = flush_observables(s);
+  if (st) return st;
   out.resize(s->nsys);
   LJ_CUDA(s, cudaMemcpyAsync(out.data(), s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
@@ -534,6 +559,8 @@ lj_status read_scalars(lj_system* s, std::vector<DevScalars>& out) {
 }
 
 lj_status write_scalars(lj_system* s, const std::vector<DevScalars>& in) {
+  lj_status st = flush_observables(s);
+  if (st) return st;
   LJ_CUDA(s, cudaMemcpyAsync(s->sc.p, in.data(), sizeof(DevScalars) * s->nsys, cudaMemcpyHostToDevice, s->stream));
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   return LJ_OK;
@@ -808,6 +835,10 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
   }
   const int mode = step_mode(s);
   const bool fused = use_fused(s);
+  if (!fused || mode != MODE_TVN) {
+    lj_status st = flush_observables(s);
+    if (st) return st;
+  }
   if (fused && (!s->pred_ready || s->pred_dt != dt)) {
     LJ_CUDA(s, launch_predict(state_args(s), nblocks(s), s->BI, s->stream));
     s->launches += 1;
@@ -828,6 +859,7 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
     LJ_CUDA(s, cudaGraphLaunch(ge->exec, s->stream));
     s->launches += ge->kernels;
     if (fused) s->qpar ^= 1;  // the step wrote the next predictor into the other buffer
+    if (fused && mode == MODE_TVN) s->obs_maybe_pending = true;
   }
   return LJ_OK;
 }
@@ -1245,6 +1277,8 @@ lj_status lj_get_stream(lj_system* s, void** stream) {
 lj_status lj_set_stream(lj_system* s, void* stream) {
   if (!s) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);
+  lj_status st = flush_observables(s);
+  if (st) return st;
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->stream = stream ? (cudaStream_t)stream : s->own_stream;
   clear_graphs(s);

@@ -47,7 +47,9 @@ def test_batch_periodic_only_uses_fused_step(ljgb_mod):
     c0 = b.launch_count()
     b.integrate(0.004, 10)
     b.sync()
-    assert b.launch_count() - c0 == 1 + 2 * 10   # predictor, then pairs + TVN close per step
+    # predictor, then pairs + TVN close per step, and the last step's
+    # observables (k_obs_finalize) at the sync
+    assert b.launch_count() - c0 == 1 + 2 * 10 + 1
     ob = b.batch_observables()
     for k, c in enumerate(cfgs):
         s = ljgb_mod.System(cfg=c)

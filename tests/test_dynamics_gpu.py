@@ -170,8 +170,10 @@ def test_launch_count_and_graph_reuse(ljgb_mod):
     s.integrate(0.005, 10)
     s.sync()
     # fused TVN, periodic: one predictor, then pair kernel (+ epilogue) and
-    # k_tvn_close per step
-    assert s.launch_count() - c0 == 1 + 2 * 10
+    # k_tvn_close per step; the last step's observables are computed by one
+    # k_obs_finalize when the host syncs (earlier steps' inside the next
+    # step's pair kernel)
+    assert s.launch_count() - c0 == 1 + 2 * 10 + 1
     c1 = s.launch_count()
     s.integrate(0.005, 10)
     assert s.launch_count() - c1 == 2 * 10     # prediction carried over from the last step
