@@ -258,7 +258,6 @@ bool calc_forces(float* Pos, float* Force, float* host_pressure, int n, float L,
   a.partial = c.partial;
   a.status = c.status;
   a.hist = HistArgs{0, kRefBins, 1.0f / dr2, 0.0f, c.hist};
-  a.minus_one = -1;
   const bool want_rdf = host_RDF != nullptr && dr2 > 0.0f;
   if (want_rdf) REF_CHECK(cudaMemsetAsync(c.hist, 0, sizeof(unsigned long long) * kRefBins, c.stream));
   REF_CHECK(launch_pairs(0, c.shape, true, want_rdf, a, c.sched.G, c.stream));

@@ -37,7 +37,6 @@ struct PairArgs {
   float* partial;             // nseg x 5 x threads  (float, or double for FP64)
   int* status;                // device status word (timeouts)
   HistArgs hist;
-  int minus_one;              // -1 (a runtime operand for the integer pipe balance)
 };
 
 

@@ -324,7 +324,6 @@ extern "C" lj_status lj_forces_static(const float* pos4, float* force4, double* 
   a.partial = partial;
   a.status = status;
   a.hist = HistArgs{0, 1, 1.0f, 0.0f, nullptr};
-  a.minus_one = -1;
   if ((e = launch_pairs(0, kShape, true, false, a, p.G, st)) != cudaSuccess)
     return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
   k_static_reduce<<<p.nblocks, kBI, 0, st>>>(partial, blocks, sc, reinterpret_cast<float4*>(force4), blk);

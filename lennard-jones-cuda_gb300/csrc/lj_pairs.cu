@@ -41,21 +41,8 @@ constexpr int kChunk = LJ_CHUNK;  // pairs per compensated force partial sum
 // tile; the unrolled chunk loop needs those to be whole chunks.
 static_assert(kSplitGrain % kChunk == 0, "schedule cuts must fall on chunk boundaries");
 
-// Wrapping difference of two fixed-point coordinates, issued as an integer
-// multiply-add by a runtime -1 so that it runs on the FMA pipe: the int->float
-// conversions already load the (half-rate) ALU pipe, and moving the three
-// subtractions off it measured 5% faster on GB300.  LJ_SUB_IADD restores the
-// plain subtraction.
-__device__ __forceinline__ int fixed_diff(int a, int b, int m1) {
-#ifndef LJ_SUB_IADD
-  int r;
-  asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(r) : "r"(b), "r"(m1), "r"(a));
-  return r;
-#else
-  (void)m1;
-  return (int)((unsigned)a - (unsigned)b);
-#endif
-}
+// Wrapping difference of two fixed-point coordinates (the minimum image).
+__device__ __forceinline__ int fixed_diff(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
 
 __device__ __forceinline__ float rcp_approx(float x) {
   float r;
@@ -68,10 +55,10 @@ __device__ __forceinline__ float rcp_approx(float x) {
 template <bool MASKED>
 __device__ __forceinline__ void pair_mixed(const int4 qi, const int4 qj, float k2inv, bool excl,
                                            float& fx, float& fy, float& fz, float& pa,
-                                           float& pb, int m1) {
-  const float dx = __int2float_rn(fixed_diff(qi.x, qj.x, m1));
-  const float dy = __int2float_rn(fixed_diff(qi.y, qj.y, m1));
-  const float dz = __int2float_rn(fixed_diff(qi.z, qj.z, m1));
+                                           float& pb) {
+  const float dx = __int2float_rn(fixed_diff(qi.x, qj.x));
+  const float dy = __int2float_rn(fixed_diff(qi.y, qj.y));
+  const float dz = __int2float_rn(fixed_diff(qi.z, qj.z));
   const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
   // r2 is in fixed-point units^2, between ~1e14 and ~1.4e19: far from the
   // subnormal and 2^126 ranges, so the raw approximate reciprocal applies.
@@ -85,6 +72,77 @@ __device__ __forceinline__ void pair_mixed(const int4 qi, const int4 qj, float k
   fz = __fmaf_rn(s, dz, fz);
   pa = __fmaf_rn(r6, r6, pa);
   pb += r6;
+}
+
+// Packed FP32x2 arithmetic (PTX .f32x2, sm_100 and later): one instruction
+// applies the operation to two independent FP32 values held in a 64-bit
+// register pair.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk2(f32x2 r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// Two pairs (i, j0) and (i, j1) as the two lanes of FP32x2 operations: the
+// same arithmetic as pair_mixed per lane, with half the instructions after
+// the int -> float conversions.  The accumulators hold the j0 and j1 partial
+// sums in their two lanes.
+// On GB300 an FP32x2 instruction occupies both FMA sub-pipes (heavy and
+// lite) for two cycles, so the FP32 throughput is that of two FFMAs; what it
+// saves is issue slots.  The scalar loop issued ~23.7 warp-instructions per
+// 32 pairs at 84% issue utilisation with the FMA pipes 64% busy; this one
+// issues ~16.8 (ncu: 1.41e8 vs 1.98e8 per N=16384 launch) and ran 4.5%
+// faster in the same step.  It needs ~80 registers, hence 6 (128-thread) or
+// 3 (256-thread) resident CTAs per SM, and the integer differences stay on
+// the ALU pipe, which has room here.
+template <bool MASKED>
+__device__ __forceinline__ void pair_mixed2(const int4 qi, const int4 qa, const int4 qb, f32x2 k2inv2, bool exa,
+                                            bool exb, f32x2& fx, f32x2& fy, f32x2& fz, f32x2& pa, f32x2& pb) {
+  const f32x2 dx = pk2(__int2float_rn(fixed_diff(qi.x, qa.x)), __int2float_rn(fixed_diff(qi.x, qb.x)));
+  const f32x2 dy = pk2(__int2float_rn(fixed_diff(qi.y, qa.y)), __int2float_rn(fixed_diff(qi.y, qb.y)));
+  const f32x2 dz = pk2(__int2float_rn(fixed_diff(qi.z, qa.z)), __int2float_rn(fixed_diff(qi.z, qb.z)));
+  const f32x2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+  float r2a, r2b;
+  upk2(r2, r2a, r2b);
+  float ra = rcp_approx(r2a), rb = rcp_approx(r2b);
+  if (MASKED) {
+    ra = exa ? 0.0f : ra;
+    rb = exb ? 0.0f : rb;
+  }
+  const f32x2 ri = mul2(pk2(ra, rb), k2inv2);
+  const f32x2 r6 = mul2(mul2(ri, ri), ri);
+  const f32x2 t = fma2(r6, pk2(12.0f, 12.0f), pk2(-6.0f, -6.0f));
+  const f32x2 sf = mul2(mul2(r6, ri), t);
+  fx = fma2(sf, dx, fx);
+  fy = fma2(sf, dy, fy);
+  fz = fma2(sf, dz, fz);
+  pa = fma2(r6, r6, pa);
+  pb = add2(pb, r6);
+}
+
+__device__ __forceinline__ float lane_sum(f32x2 v) {
+  float a, b;
+  upk2(v, a, b);
+  return a + b;
 }
 
 // Histogram bin of a pair from its fixed-point separation; the arithmetic is
@@ -180,7 +238,6 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
   int4 qi = a.q[bi.p0 + (valid_i ? i_local : bi.i0)];
   float k2inv = a.sc[bi.sys].k2inv;
   float k2 = a.sc[bi.sys].k2;
-  const int m1 = a.minus_one;
   FloatAcc acc[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
@@ -221,17 +278,20 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           const bool diag = masked;
 #pragma unroll 1
           for (int c0 = jlo; c0 < jhi; c0 += kChunk) {
-            float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
+            const f32x2 k2i2 = pk2(k2inv, k2inv);
+            f32x2 FX = 0ull, FY = 0ull, FZ = 0ull, PA = 0ull, PB = 0ull;
             if (!diag) {
 #pragma unroll
-              for (int jj = c0; jj < c0 + kChunk; ++jj)
-                pair_mixed<false>(qi, st[jj], k2inv, false, fx, fy, fz, pa, pb, m1);
+              for (int jj = c0; jj < c0 + kChunk; jj += 2)
+                pair_mixed2<false>(qi, st[jj], st[jj + 1], k2i2, false, false, FX, FY, FZ, PA, PB);
             } else {
               const int self = i_local - j0;  // tile-local index of this thread's i
 #pragma unroll
-              for (int jj = c0; jj < c0 + kChunk; ++jj)
-                pair_mixed<true>(qi, st[jj], k2inv, jj == self, fx, fy, fz, pa, pb, m1);
+              for (int jj = c0; jj < c0 + kChunk; jj += 2)
+                pair_mixed2<true>(qi, st[jj], st[jj + 1], k2i2, jj == self, jj + 1 == self, FX, FY, FZ, PA, PB);
             }
+            const float fx = lane_sum(FX), fy = lane_sum(FY), fz = lane_sum(FZ), pa = lane_sum(PA),
+                        pb = lane_sum(PB);
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);
@@ -244,7 +304,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
             float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
             const int c1 = min(jhi, c0 + kChunk);
             for (int jj = c0; jj < c1; ++jj)
-              pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb, m1);
+              pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb);
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);
@@ -553,12 +613,12 @@ cudaError_t occupancy_fp64_t(int* blocks_per_sm) {
 // Kernel shapes the autotuner chooses among (threads = i-block size; MINB =
 // resident CTAs per SM the register allocation must allow).
 #define LJ_SHAPES(X)   \
-  X(0, 128, 256, 3, 8)  \
-  X(1, 64, 256, 3, 16)  \
-  X(2, 256, 256, 3, 4)  \
-  X(3, 128, 512, 2, 8)  \
-  X(4, 128, 512, 3, 8)  \
-  X(5, 256, 512, 3, 4)
+  X(0, 128, 256, 3, 6)  \
+  X(1, 128, 512, 3, 6)  \
+  X(2, 256, 256, 3, 3)  \
+  X(3, 256, 512, 3, 3)  \
+  X(4, 256, 256, 3, 2)  \
+  X(5, 64, 256, 3, 12)
 
 const PairShape kShapes[] = {
 #define LJ_SHAPE_ROW(i, T, TL, S, M) {T, TL, S},

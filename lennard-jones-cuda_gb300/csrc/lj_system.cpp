@@ -181,7 +181,6 @@ PairArgs pair_args(lj_system* s) {
   a.partial = s->partial.p;
   a.status = s->status.p;
   a.hist = HistArgs{0, 1, 1.0f, 0.0f, nullptr};
-  a.minus_one = -1;
   return a;
 }
 
