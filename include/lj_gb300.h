@@ -267,6 +267,35 @@ lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_
 lj_status lj_forces_static(const float* pos4, float* force4, double* sums, int32_t n, float box,
                            int32_t periodic, void* stream);
 
+/* ---- Per-step subsystem counts and summed RDF (task drivers) --------------
+ * The fluctuation task of the reference (src/tasks/run-fluctuations/
+ * run-fluctuations.cpp:87-174 with run-fluctuations-aux.h:124-273) counts,
+ * after every step, the particles of nested subsystems and averages the RDF;
+ * it copies all positions to the host for that every step.  Here the counts
+ * are made on the GPU after every lj_step step into a ring that the host
+ * reads every few hundred steps.  Single-box handles only. */
+typedef struct {
+  int32_t type;       /* 0/1/2: slab x/y/z < alpha L (GetNSubsystemBatch types 0-2);
+                         3: cube of volume alpha L^3 around the box centre (type 3);
+                         4/5/6: |v_x|/|v_y|/|v_z| < alpha vmax (GetNsubVzBatch types 0-2) */
+  int32_t nalpha;     /* alpha_k = (k+1) alpha_step, k < nalpha (<= 64) */
+  double alpha_step;
+  double vmax;        /* types 4-6 (the reference uses 3 sqrt(T0)) */
+} lj_counter;
+/* Enables the counters (ncounters = 0 disables them); ring_steps rows are
+ * kept between reads. */
+lj_status lj_counters_configure(lj_system* sys, const lj_counter* counters, int32_t ncounters, int32_t ring_steps);
+/* Copies the rows of the steps since the last read, oldest first: per step
+ * and counter, the cumulative counts N(alpha_0) .. N(alpha_{nalpha-1}).  With
+ * counts = NULL only *nsteps is set.  More steps than ring_steps since the
+ * last read is an error (LJ_ERR_INVALID) and drops them. */
+lj_status lj_counters_read(lj_system* sys, int32_t* counts, int32_t max_steps, int32_t* nsteps);
+/* Adds the RDF counts (modes and bins as lj_rdf_counts) of the state after
+ * every step into a device histogram; enable = 0 stops and clears. */
+lj_status lj_rdf_accumulate(lj_system* sys, int32_t enable, int32_t mode, int32_t nbins, double width);
+/* The summed counts and the number of steps summed; reset != 0 clears both. */
+lj_status lj_rdf_accumulated(lj_system* sys, uint64_t* counts, int64_t* nsamples, int32_t reset);
+
 /* ---- Differentiable MD (adjoint) ----------------------------------------
  * No counterpart in the reference (its dynamics are not differentiable).
  * Gradients of a time-averaged trajectory loss

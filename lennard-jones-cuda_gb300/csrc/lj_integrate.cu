@@ -404,6 +404,50 @@ __global__ void k_obs_finalize(StateArgs s) {
   pending_observables(s, blockIdx.x, gridDim.x, sh);
 }
 
+// Subsystem counters of the fluctuation task (run-fluctuations-aux.h:124-273,
+// GetNSubsystemBatch / GetNsubVzBatch): per particle and counter, the index
+// of the first alpha whose subsystem contains it; the host turns the
+// histogram into cumulative counts N(alpha_k).
+//   slab (type t < 3):  k = (int)((x_t / L) / alpha_step)
+//   cube (type 3):      k = max over axes of #{tl_j <= |x_c - L/2| / 0.5}
+//   velocity (4 .. 6):  k = (int)((|v_c| / vmax) / alpha_step)
+__global__ void k_counters(StateArgs s, const CounterDev* cs, int nc, int nbins, int* row, int n) {
+  extern __shared__ int shc[];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) shc[b] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double L = s.boxes[0].L;
+    double x[3], v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      x[c] = s.x[(size_t)c * s.npad + i];
+      v[c] = s.v[(size_t)c * s.npad + i];
+    }
+    for (int q = 0; q < nc; ++q) {
+      const CounterDev& cd = cs[q];
+      int k;
+      if (cd.type < 3) {
+        k = (int)((x[cd.type] / L) / cd.alpha_step);
+      } else if (cd.type == 3) {
+        k = 0;
+        for (int c = 0; c < 3; ++c) {
+          const double d = fabs(x[c] - 0.5 * L) / 0.5;
+          int kc = 0;
+          while (kc < cd.nalpha && cd.tl[kc] <= d) ++kc;
+          k = kc > k ? kc : k;
+        }
+      } else {
+        k = (int)((fabs(v[cd.type - 4]) / cd.vmax) / cd.alpha_step);
+      }
+      if (k >= 0 && k < cd.nalpha) atomicAdd(&shc[cd.bin0 + k], 1);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    if (shc[b]) atomicAdd(row + b, shc[b]);
+}
+
 // |v| histogram (MDSystem.cpp:658-662): b = floor(sqrt(v.v)/step), b < nb.
 // Products and sums rounded separately so the bins are reproducible on a CPU.
 __global__ void k_velocity_hist(StateArgs s, double step, int nb, unsigned long long* counts) {
@@ -525,6 +569,13 @@ cudaError_t launch_observables(const StateArgs& s, int nsys, int mode, cudaStrea
 
 cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t st) {
   k_predict<<<nblocks, bi, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* row, int n,
+                            cudaStream_t st) {
+  const int threads = 256;
+  k_counters<<<(n + threads - 1) / threads, threads, sizeof(int) * nbins, st>>>(s, cs, nc, nbins, row, n);
   return cudaGetLastError();
 }
 

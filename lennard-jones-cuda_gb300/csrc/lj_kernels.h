@@ -110,6 +110,22 @@ cudaError_t launch_velocity_hist(const StateArgs& s, int nblocks, int bi, double
 cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
 cudaError_t launch_tvn_close(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
 cudaError_t launch_obs_finalize(const StateArgs& s, int nsys, cudaStream_t st);
+
+// Subsystem counters of the fluctuation runs (lj_counters_configure).
+constexpr int kMaxCounterAlphas = 64;
+struct CounterDev {
+  int type;    // 0/1/2 slab x/y/z < alpha L; 3 cube around the centre; 4/5/6 |v_x|/|v_y|/|v_z| < alpha vmax
+  int nalpha;  // alphas k = 0 .. nalpha-1
+  int bin0;    // first bin of this counter in the per-step row
+  int pad;
+  double alpha_step;
+  double vmax;
+  double tl[kMaxCounterAlphas];  // type 3: cube sides L alpha_k^(1/3)
+};
+// Histogram of the counters' bin indices over the particles of box 0, added
+// into row[0 .. nbins) (zeroed by the caller).
+cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* row, int n,
+                            cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,

@@ -97,6 +97,20 @@ struct lj_system {
   DevBuf<unsigned long long> hist;
   int rec_cap = 0;
 
+  // per-step subsystem counters (lj_counters_configure): one row of
+  // counter_bins ints per step in a ring of counter_cap rows
+  std::vector<CounterDev> counters;
+  DevBuf<CounterDev> dcounters;
+  DevBuf<int> counter_ring;
+  int counter_bins = 0, counter_cap = 0;
+  long long counter_head = 0, counter_tail = 0;  // rows written / rows read
+  // RDF summed over steps (lj_rdf_accumulate), from its own shadow buffer
+  bool rdf_acc = false;
+  HistArgs rdf_args{};
+  DevBuf<unsigned long long> rdf_sum;
+  DevBuf<int4> qhist;
+  long long rdf_samples = 0;
+
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
 
@@ -478,6 +492,34 @@ lj_status flush_observables(lj_system* s) {
   return LJ_OK;
 }
 
+// Work after every step: the subsystem counters and the summed RDF, when
+// enabled (plain launches after the step's graph).
+lj_status after_step(lj_system* s) {
+  if (s->counter_cap > 0) {
+    int* row = s->counter_ring.p + (size_t)(s->counter_head % s->counter_cap) * s->counter_bins;
+    LJ_CUDA(s, cudaMemsetAsync(row, 0, sizeof(int) * s->counter_bins, s->stream));
+    LJ_CUDA(s, launch_counters(state_args(s), s->dcounters.p, (int)s->counters.size(), s->counter_bins, row,
+                               s->ntotal, s->stream));
+    s->counter_head += 1;
+    s->launches += 1;
+  }
+  if (s->rdf_acc) {
+    // The step's shadow buffer holds the next step's prediction: quantize the
+    // current positions into a buffer of their own.
+    StateArgs a = state_args(s);
+    a.q = s->qhist.p;
+    LJ_CUDA(s, launch_quantize(a, nblocks(s), s->BI, false, s->stream));
+    PairArgs p = pair_args(s);
+    p.q = s->qhist.p;
+    p.hist = s->rdf_args;
+    const int shape = (s->prec == LJ_PREC_MIXED) ? s->shape : 0;
+    LJ_CUDA(s, launch_pairs(LJ_PREC_MIXED, shape, false, true, p, s->sched.G, s->stream));
+    s->rdf_samples += 1;
+    s->launches += 2;
+  }
+  return LJ_OK;
+}
+
 lj_status check_status(lj_system* s) {
   lj_status fst = flush_observables(s);
   if (fst) return fst;
@@ -729,6 +771,10 @@ lj_status lj_destroy(lj_system* s) {
   s->glob_cnt.free();
   s->blocks.free();
   s->cta_tile_begin.free();
+  s->dcounters.free();
+  s->counter_ring.free();
+  s->rdf_sum.free();
+  s->qhist.free();
   s->cta_lo.free();
   s->cta_block.free();
   s->cta_jt.free();
@@ -859,6 +905,10 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
     s->launches += ge->kernels;
     if (fused) s->qpar ^= 1;  // the step wrote the next predictor into the other buffer
     if (fused && mode == MODE_TVN) s->obs_maybe_pending = true;
+    if (s->counter_cap > 0 || s->rdf_acc) {
+      lj_status ast = after_step(s);
+      if (ast) return ast;
+    }
   }
   return LJ_OK;
 }
@@ -895,6 +945,8 @@ lj_status lj_set_recording(lj_system* s, int32_t cap) {
   if (!s || cap < 0) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  const DevRecord* old_records = s->records.p;
+  const int old_cap = s->rec_cap;
   LJ_CUDA(s, s->records.alloc((size_t)cap * s->nsys));
   s->rec_cap = cap;
   std::vector<DevScalars> sc;
@@ -904,7 +956,7 @@ lj_status lj_set_recording(lj_system* s, int32_t cap) {
     d.rec_cap = cap;
     d.rec_count = 0;
   }
-  clear_graphs(s);  // records pointer / stride are captured
+  if (s->records.p != old_records || cap != old_cap) clear_graphs(s);  // records pointer / stride are captured
   return write_scalars(s, sc);
 }
 
@@ -1118,6 +1170,128 @@ lj_status lj_velocity_counts(lj_system* s, double step, int32_t nbins, uint64_t*
   LJ_CUDA(s, cudaMemcpyAsync(counts, s->hist.p, sizeof(unsigned long long) * nbins, cudaMemcpyDeviceToHost,
                              s->stream));
   return check_status(s);
+}
+
+lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_t ncounters, int32_t ring_steps) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->counters.clear();
+  s->counter_cap = 0;
+  s->counter_bins = 0;
+  s->counter_head = s->counter_tail = 0;
+  if (ncounters == 0) return LJ_OK;
+  if (!counters || ncounters < 0) return fail(s, LJ_ERR_INVALID, "counters must be non-NULL");
+  if (ring_steps < 1) return fail(s, LJ_ERR_INVALID, "ring_steps must be >= 1");
+  if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "subsystem counters apply to single-box handles");
+  const double L = s->boxes[0].L;
+  int bins = 0;
+  for (int q = 0; q < ncounters; ++q) {
+    const lj_counter& c = counters[q];
+    if (c.type < 0 || c.type > 6) return fail(s, LJ_ERR_INVALID, "counter %d: unknown type %d", q, c.type);
+    if (c.nalpha < 1 || c.nalpha > kMaxCounterAlphas)
+      return fail(s, LJ_ERR_INVALID, "counter %d: nalpha must be in [1, %d]", q, kMaxCounterAlphas);
+    if (!(c.alpha_step > 0)) return fail(s, LJ_ERR_INVALID, "counter %d: alpha_step must be > 0", q);
+    if (c.type >= 4 && !(c.vmax > 0)) return fail(s, LJ_ERR_INVALID, "counter %d: vmax must be > 0", q);
+    CounterDev d{};
+    d.type = c.type;
+    d.nalpha = c.nalpha;
+    d.bin0 = bins;
+    d.alpha_step = c.alpha_step;
+    d.vmax = c.vmax;
+    // cube sides from the accumulated alphas, as the reference's loop forms them
+    double alpha = c.alpha_step;
+    for (int k = 0; k < c.nalpha; ++k, alpha += c.alpha_step) d.tl[k] = L * std::pow(alpha, 1. / 3.);
+    s->counters.push_back(d);
+    bins += c.nalpha;
+  }
+  s->counter_bins = bins;
+  LJ_CUDA(s, s->dcounters.alloc(s->counters.size()));
+  LJ_CUDA(s, s->counter_ring.alloc((size_t)bins * ring_steps));
+  LJ_CUDA(s, cudaMemcpy(s->dcounters.p, s->counters.data(), sizeof(CounterDev) * s->counters.size(),
+                        cudaMemcpyHostToDevice));
+  s->counter_cap = ring_steps;
+  return LJ_OK;
+}
+
+lj_status lj_counters_read(lj_system* s, int32_t* counts, int32_t max_steps, int32_t* nsteps) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  const long long avail = s->counter_head - s->counter_tail;
+  if (nsteps) *nsteps = (int32_t)std::min<long long>(avail, INT32_MAX);
+  if (avail > s->counter_cap) {
+    s->counter_tail = s->counter_head;
+    return fail(s, LJ_ERR_INVALID, "%lld steps since the last read overflowed the counter ring of %d steps", avail,
+                s->counter_cap);
+  }
+  if (!counts) return LJ_OK;
+  const int n = (int)std::min<long long>(avail, max_steps);
+  const int B = s->counter_bins;
+  for (int k = 0; k < n; ++k) {
+    const long long row = (s->counter_tail + k) % s->counter_cap;
+    LJ_CUDA(s, cudaMemcpyAsync(counts + (size_t)k * B, s->counter_ring.p + (size_t)row * B, sizeof(int) * B,
+                               cudaMemcpyDeviceToHost, s->stream));
+  }
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  // cumulative over each counter's alphas: N(alpha_k) = sum of bins <= k
+  for (int k = 0; k < n; ++k)
+    for (const CounterDev& d : s->counters) {
+      int32_t* r = counts + (size_t)k * B + d.bin0;
+      for (int a = 1; a < d.nalpha; ++a) r[a] += r[a - 1];
+    }
+  s->counter_tail += n;
+  if (nsteps) *nsteps = n;
+  return LJ_OK;
+}
+
+lj_status lj_rdf_accumulate(lj_system* s, int32_t enable, int32_t mode, int32_t nbins, double width) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->rdf_acc = false;
+  s->rdf_samples = 0;
+  if (!enable) return LJ_OK;
+  if (mode < 0 || mode > 2) return fail(s, LJ_ERR_INVALID, "unknown RDF mode %d", mode);
+  if (nbins < 1 || nbins > kMaxHistBins) return fail(s, LJ_ERR_INVALID, "nbins must be in [1, %d]", kMaxHistBins);
+  if (!(width > 0)) return fail(s, LJ_ERR_INVALID, "bin width must be > 0");
+  if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "RDF accumulation applies to single-box handles");
+  LJ_CUDA(s, s->rdf_sum.alloc(nbins));
+  LJ_CUDA(s, s->qhist.alloc(s->npad));
+  LJ_CUDA(s, cudaMemset(s->rdf_sum.p, 0, sizeof(unsigned long long) * nbins));
+  HistArgs h{};
+  h.mode = mode;
+  h.nb = nbins;
+  const double sig = s->cfg[0].sigma;
+  if (mode == 2) {
+    h.inv_w = (float)(sig / width);
+    const double rmax = nbins * width / sig;
+    h.rmax2 = (float)(rmax * rmax);
+  } else {
+    h.inv_w = (float)(sig * sig / width);
+    h.rmax2 = 0.0f;
+  }
+  h.counts = s->rdf_sum.p;
+  s->rdf_args = h;
+  s->rdf_acc = true;
+  return LJ_OK;
+}
+
+lj_status lj_rdf_accumulated(lj_system* s, uint64_t* counts, int64_t* nsamples, int32_t reset) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  if (!s->rdf_acc) return fail(s, LJ_ERR_INVALID, "RDF accumulation is not enabled");
+  if (counts)
+    LJ_CUDA(s, cudaMemcpy(counts, s->rdf_sum.p, sizeof(unsigned long long) * s->rdf_args.nb, cudaMemcpyDeviceToHost));
+  if (nsamples) *nsamples = s->rdf_samples;
+  if (reset) {
+    LJ_CUDA(s, cudaMemset(s->rdf_sum.p, 0, sizeof(unsigned long long) * s->rdf_args.nb));
+    s->rdf_samples = 0;
+  }
+  return LJ_OK;
 }
 
 lj_status lj_tune_info(lj_system* s, int32_t* nshapes, int32_t* active, int32_t k, int32_t* threads, int32_t* ipt,

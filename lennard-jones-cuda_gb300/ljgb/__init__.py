@@ -56,6 +56,11 @@ class Observables(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class Counter(C.Structure):
+    """lj_counter (include/lj_gb300.h): type 0-2 slab, 3 cube, 4-6 |v| component."""
+    _fields_ = [("type", C.c_int32), ("nalpha", C.c_int32), ("alpha_step", C.c_double), ("vmax", C.c_double)]
+
+
 _lib = None
 _P = C.c_void_p
 _dp = C.POINTER(C.c_double)
@@ -117,6 +122,10 @@ def _declare(L):
                                     C.c_float, C.c_int, C.c_int]),
         "threadSync": (None, []),
         "threadExit": (None, []),
+        "lj_counters_configure": (C.c_int, [_P, _P, C.c_int32, C.c_int32]),
+        "lj_counters_read": (C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_int32)]),
+        "lj_rdf_accumulate": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
+        "lj_rdf_accumulated": (C.c_int, [_P, _P, C.POINTER(C.c_int64), C.c_int32]),
         "lj_adjoint_create": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(_P)]),
         "lj_adjoint_destroy": (C.c_int, [_P]),
         "lj_adjoint_last_error": (C.c_char_p, [_P]),
@@ -373,6 +382,30 @@ class System:
     # -- tuning / profiling ----------------------------------------------
     def autotune(self):
         self._c(load().lj_autotune(self.h))
+
+    def counters_configure(self, counters, ring_steps: int = 1000):
+        """counters: sequence of (type, nalpha, alpha_step, vmax)."""
+        arr = (Counter * max(1, len(counters)))(*[Counter(*c) for c in counters])
+        self.counter_bins = sum(int(c[1]) for c in counters)
+        self._c(load().lj_counters_configure(self.h, arr, len(counters), int(ring_steps)))
+
+    def counters_read(self, max_steps: int = 1 << 20):
+        n = C.c_int32()
+        self._c(load().lj_counters_read(self.h, None, 0, C.byref(n)))
+        m = min(n.value, max_steps)
+        out = np.zeros((m, self.counter_bins), np.int32)
+        self._c(load().lj_counters_read(self.h, out.ctypes.data, m, C.byref(n)))
+        return out[:n.value]
+
+    def rdf_accumulate(self, enable: bool, mode: int = 2, nbins: int = 200, width: float = 0.05):
+        self._rdf_nbins = nbins
+        self._c(load().lj_rdf_accumulate(self.h, int(bool(enable)), mode, nbins, width))
+
+    def rdf_accumulated(self, reset: bool = False):
+        out = np.zeros(self._rdf_nbins, np.uint64)
+        n = C.c_int64()
+        self._c(load().lj_rdf_accumulated(self.h, out.ctypes.data, C.byref(n), int(bool(reset))))
+        return out, n.value
 
     def set_kernel_shape(self, shape: int):
         self._c(load().lj_set_kernel_shape(self.h, int(shape)))

@@ -62,7 +62,7 @@ def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    for d in (CSRC, INCLUDE):
+    for d in (CSRC, INCLUDE, os.path.join(PKG_DIR, "tasks")):
         for root, _, files in os.walk(d):
             for f in files:
                 if os.path.getmtime(os.path.join(root, f)) > t:
@@ -97,7 +97,36 @@ def _build_into(lib_path: str, verbose: bool) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, lib_path)
+    if lib_path == LIB_PATH:
+        build_tasks()
     return lib_path
+
+
+TASKS = {"ljgb-run-isotherm": "run_isotherm.cpp", "ljgb-run-fluctuations": "run_fluctuations.cpp"}
+TASK_DIR = os.path.join(PKG_DIR, "tasks")
+BIN_DIR = os.path.join(PKG_DIR, "bin")
+
+
+def build_tasks() -> list:
+    """The task-driver executables (C++ over the lj_* ABI), next to the
+    library in lennard-jones-cuda_gb300/bin/."""
+    os.makedirs(BIN_DIR, exist_ok=True)
+    cxx = shutil.which("g++") or "g++"
+    outs = []
+
+    def one(item):
+        name, src = item
+        out = os.path.join(BIN_DIR, name)
+        cmd = [cxx, "-std=c++17", "-O2", "-I", INCLUDE, os.path.join(TASK_DIR, src), "-o", out, "-L", PKG_DIR,
+               "-llj_gb300", "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("task build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+        return out
+
+    with cf.ThreadPoolExecutor(max_workers=len(TASKS)) as ex:
+        outs = list(ex.map(one, TASKS.items()))
+    return outs
 
 
 if __name__ == "__main__":

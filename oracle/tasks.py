@@ -1,0 +1,88 @@
+"""numpy restatement of the reference's task-driver statistics (test
+infrastructure only: tests/ import it as the checker; the product library
+never imports, links or calls it).
+
+  * subsystem_counts: GetNSubsystemBatch
+    (src/tasks/run-fluctuations/include/run-fluctuations-aux.h:186-240);
+  * velocity_counts: GetNsubVzBatch (run-fluctuations-aux.h:242-273);
+  * NumberStatistics moments / mean error / scaled variance and its error
+    (src/extra/sample-moments/NumberStatistics.h: moments from sums of N^k,
+    error of the mean sqrt(var/n), central-moment covariances after Kendall &
+    Stuart, scaled variance kappa_2/<N>);
+  * TimeAverage statistical inefficiency s = 2 / ln(var / (<N_t N_{t-1}> -
+    <N>^2)), s = 1 if negative (src/tasks/auxiliary/time-average-aux.h:27-67,
+    after Allen & Tildesley, Computer Simulation of Liquids, pp. 194-195).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def alphas(step, upper_inclusive):
+    """The reference's alpha loop: alpha = step, 2 step, ... accumulated in
+    floating point, < 1 - 1e-9 (coordinates) or <= 1 + 1e-9 (velocities)."""
+    out = []
+    a = step
+    while (a <= 1.0 + 1e-9) if upper_inclusive else (a < 1.0 - 1e-9):
+        out.append(a)
+        a += step
+    return out
+
+
+def subsystem_counts(pos, L, alpha_step, type_):
+    """Cumulative counts N(alpha_k) for type 0/1/2 (slab) or 3 (central cube)."""
+    al = alphas(alpha_step, False)
+    cnts = np.zeros(len(al), np.int64)
+    if type_ == 3:
+        tls = np.array([L * a ** (1.0 / 3.0) for a in al])
+        d = np.abs(pos - 0.5 * L) / 0.5
+        ind = np.searchsorted(tls, d, side="right").max(axis=1)
+    else:
+        ind = ((pos[:, type_] / L) / alpha_step).astype(np.int64)
+    for k in ind:
+        if 0 <= k < len(al):
+            cnts[k] += 1
+    return np.cumsum(cnts)
+
+
+def velocity_counts(vel, vmax, alpha_step, component):
+    al = alphas(alpha_step, True)
+    cnts = np.zeros(len(al), np.int64)
+    ind = ((np.abs(vel[:, component]) / vmax) / alpha_step).astype(np.int64)
+    for k in ind:
+        if 0 <= k < len(al):
+            cnts[k] += 1
+    return np.cumsum(cnts)
+
+
+def moments(x):
+    """mean, biased variance, error of the mean, scaled variance and its error."""
+    x = np.asarray(x, np.float64)
+    n = len(x)
+    m = x.mean()
+    mu = [np.mean((x - m) ** k) for k in range(5)]
+    var = mu[2]
+    mean_err = np.sqrt(var / n)
+    # cov(m2, m2) = (mu4 - mu2^2)/n; cov(m2, mean) = mu3/n (Kendall & Stuart)
+    c1, c2 = var, m
+    c1dev = (mu[4] - mu[2] ** 2) / n
+    c2dev = mean_err ** 2
+    c12 = mu[3] / n
+    w = c1 / c2
+    w_err = abs(w) * np.sqrt(c1dev / c1 / c1 + c2dev / c2 / c2 - 2.0 * c12 / c1 / c2)
+    return dict(mean=m, var=var, mean_err=mean_err, w=w, w_err=w_err)
+
+
+def inefficiency(x):
+    """s = 2 / ln(var / corr), s = 1 if negative; also s = 1 where corr <= 0
+    or var / corr <= 1, where the reference's formula gives NaN / infinity
+    (a deliberate difference, stated in include/ljgb/Statistics.hpp)."""
+    x = np.asarray(x, np.float64)
+    n = len(x)
+    m = x.mean()
+    var = np.mean(x * x) - m * m
+    corr = np.sum(x[1:] * x[:-1]) / (n - 1) - m * m
+    if not corr > 0 or not var / corr > 1:
+        return 1.0
+    s = 2.0 / np.log(var / corr)
+    return 1.0 if s < 0 else s

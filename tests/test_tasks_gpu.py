@@ -1,0 +1,141 @@
+"""Task-driver support on the GPU: the per-step subsystem counters and the
+RDF summed over steps, against the numpy restatement of the reference's
+counting functions (oracle/tasks.py) and the exact RDF emulation, on the
+positions and velocities of the same steps."""
+import numpy as np
+import pytest
+
+import lj_testutil as U
+
+pytestmark = pytest.mark.gpu
+
+
+def test_subsystem_counters_match_reference_counting(ljgb_mod):
+    import tasks
+    N, rho, T0 = 400, 0.05, 1.4
+    s = ljgb_mod.System(n=N, density=rho, temperature=T0, canonical=1, precision=ljgb_mod.PREC_FP64)
+    vmax = 3.0 * np.sqrt(T0)
+    spec = [(0, 19, 0.05, 0.0), (1, 19, 0.05, 0.0), (2, 19, 0.05, 0.0), (3, 19, 0.05, 0.0),
+            (6, 20, 0.05, vmax), (2, 1, 0.5, 0.0)]
+    s.counters_configure(spec, ring_steps=16)
+    expect = []
+    for _ in range(6):
+        s.integrate(0.005)
+        p, v, _ = s.get_state()
+        row = np.concatenate([tasks.subsystem_counts(p, s.L, 0.05, t) for t in range(4)] +
+                             [tasks.velocity_counts(v, vmax, 0.05, 2), tasks.subsystem_counts(p, s.L, 0.5, 2)[:1]])
+        expect.append(row)
+    got = s.counters_read()
+    assert got.shape == (6, 19 * 4 + 20 + 1)
+    assert np.array_equal(got, np.array(expect))
+    assert s.counters_read().shape[0] == 0          # read clears
+    # the cube of volume fraction 1 holds nothing beyond the box: last alpha < 1
+    assert got[:, 3 * 19 + 18].max() <= N
+
+
+def test_counter_ring_overflow_is_reported(ljgb_mod):
+    s = ljgb_mod.System(n=256, density=0.5, temperature=1.0)
+    s.counters_configure([(0, 4, 0.25, 0.0)], ring_steps=4)
+    s.integrate(0.005, 6)
+    with pytest.raises(ljgb_mod.LJError):
+        s.counters_read()
+    s.integrate(0.005, 3)
+    assert s.counters_read().shape == (3, 4)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["mixed", "fp64"])
+def test_rdf_summed_over_steps(ljgb_mod, oracle_mod, prec):
+    N, rho = 1000, 0.7
+    s = ljgb_mod.System(n=N, density=rho, temperature=1.0, canonical=1, precision=prec, lattice=1, jitter=0.02)
+    nb, w = 167, 0.03
+    s.rdf_accumulate(True, ljgb_mod.RDF_R_LINEAR, nb, w)
+    want = np.zeros(nb, np.uint64)
+    ks = s.L / 4294967296.0
+    for _ in range(3):
+        s.integrate(0.005)
+        p, _, _ = s.get_state()
+        want += oracle_mod.emu_rdf_r(oracle_mod.emu_fixed(p, s.L), np.float32(ks * ks), np.float32(1.0 / w),
+                                     np.float32((nb * w) ** 2), nb).astype(np.uint64)
+    got, n = s.rdf_accumulated(reset=True)
+    assert n == 3
+    assert np.array_equal(got, want)
+    s.integrate(0.005, 2)
+    assert s.rdf_accumulated()[1] == 2
+
+
+def _run_task(name, text, tmp_path):
+    import os
+    import subprocess
+    import ljgb.build as b
+    f = tmp_path / "params.txt"
+    f.write_text(text)
+    r = subprocess.run([os.path.join(b.BIN_DIR, name), str(f)], cwd=tmp_path, capture_output=True, text=True,
+                       timeout=900)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r
+
+
+def _table(path):
+    return np.loadtxt(path, skiprows=1, ndmin=2)
+
+
+def test_run_isotherm_driver(ljlib, tmp_path):
+    """Three TVN densities at T*=1.4 (N=256), 2 tau equilibration, 6 tau
+    production: one row per density with the reference's columns."""
+    r = _run_task("ljgb-run-isotherm", "# isotherm\nN 256\nT* 1.4\nrho*_min 0.1\nrho*_max 0.31\ndrho* 0.1\n"
+                  "teq 2.\ntfin 8.\ndt* 0.004\nuseCUDA 1\noutput_prefix iso\n", tmp_path)
+    files = list(tmp_path.glob("iso.*.N256.Tst1.4.dat"))
+    assert len(files) == 1
+    head = files[0].read_text().splitlines()[0].split()
+    assert head == ["rho*", "t*", "T*", "<u*>", "d<u*>", "teq_u*", "<p*>", "d<p*>", "teq_p*", "<Z>", "d<Z>",
+                    "w[N]", "dw[N]"]
+    t = _table(files[0])
+    assert t.shape == (3, 13)
+    assert np.allclose(t[:, 0], [0.1, 0.2, 0.3])
+    assert np.allclose(t[:, 1], 8.0 - 0.004, atol=0.005)
+    assert np.all(np.abs(t[:, 2] - 1.4) < 0.15)                      # TVN holds T* near 1.4
+    assert np.all(np.isfinite(t)) and np.all(t[:, [4, 7, 10]] > 0)   # errors
+    assert np.all(np.diff(t[:, 6]) > 0)                              # p* rises with density
+    assert np.all((t[:, 9] > 0.5) & (t[:, 9] < 1.2))                 # Z of a dilute-to-moderate LJ gas at T*=1.4
+    # a console line every 1000 observations (1500 per density)
+    assert sum(1 for line in r.stdout.splitlines() if line.split()[:1] and line.split()[0] in ("0.1", "0.2", "0.3")) == 3
+
+
+@pytest.mark.parametrize("ensemble", ["tvn", "evn"])
+def test_run_fluctuations_driver(ljlib, tmp_path, ensemble):
+    """N=400 fluctuation run (the sample inputs' N and u*), 2000 production
+    steps: the time-dependence table, the averaged RDF and the five
+    fluctuation tables with the reference's layout."""
+    canon = "1" if ensemble == "tvn" else "0"
+    _run_task("ljgb-run-fluctuations", "N 400\nT* 1.4\nu* 1.708\nrho* 0.3\nteq 1.\ntfin 9.\ndt* 0.004\n"
+              "canonical %s\nsubvolume_spacing 0.05\noutput_prefix fl\n" % canon, tmp_path)
+    key = "Tst1.4" if ensemble == "tvn" else "ust1.708"
+    pre = list(tmp_path.glob("fl.*.N400.%s.rhost0.3.TimeDep.txt" % key))
+    assert len(pre) == 1
+    base = str(pre[0])[:-len(".TimeDep.txt")]
+    td = _table(base + ".TimeDep.txt")
+    assert td.shape == (2, 13)
+    assert np.allclose(td[:, 0], [1.0 + 4.0, 1.0 + 8.0], atol=0.01)
+    if ensemble == "evn":
+        assert np.allclose(td[:, 1], 1.708, atol=2e-3)            # energy per particle conserved
+    else:
+        assert np.all(np.abs(td[:, 2] - 1.4) < 0.15)
+    assert np.all(np.abs(td[:, 10:13]) < 1e-6)                     # zero net momentum
+    g = _table(base + ".RDF.dat")
+    assert g.shape == (256, 2)
+    r, gr = g[:, 0], g[:, 1]
+    assert np.all(gr[r < 0.8] < 1e-3)                               # hard core
+    far = (r > 2.5) & (r < 3.5)
+    assert abs(gr[far].mean() - 1.0) < 0.15                         # g(r) -> 1
+    assert 1.2 < gr.max() < 4.0                                     # first shell
+    for ax in "XYZ":
+        f = _table(base + ".flucs%s.dat" % ax)
+        assert f.shape == (19, 6)
+        assert np.allclose(f[:, 1], f[:, 0] * 400, rtol=0.15, atol=4)  # <N> ~ alpha N
+        assert np.all((f[:, 3] > 0.05) & (f[:, 3] < 5))              # w[N]/(1-alpha)
+    cube = _table(base + ".flucsCube.dat")
+    assert cube.shape == (19, 6) and np.all(np.diff(cube[:, 1]) > 0)
+    vz = _table(base + ".flucsVz.dat")
+    assert vz.shape == (20, 7)
+    assert np.allclose(vz[:, 0], np.sqrt(1.4) * 3 * 0.05 * np.arange(1, 21), rtol=1e-9)
+    assert np.all(np.diff(vz[:, 1]) >= 0) and vz[-1, 2] > 0.98         # nearly all |v_z| < 3 sqrt(T)
