@@ -96,7 +96,8 @@ def test_run_isotherm_driver(ljlib, tmp_path):
     assert np.all(np.abs(t[:, 2] - 1.4) < 0.15)                      # TVN holds T* near 1.4
     assert np.all(np.isfinite(t)) and np.all(t[:, [4, 7, 10]] > 0)   # errors
     assert np.all(np.diff(t[:, 6]) > 0)                              # p* rises with density
-    assert np.all((t[:, 9] > 0.5) & (t[:, 9] < 1.2))                 # Z of a dilute-to-moderate LJ gas at T*=1.4
+    # near-critical isotherm (T*=1.4, T_c ~ 1.3): Z = p/(rho T) falls from ~0.7 at rho*=0.1 to ~0.5 at 0.3
+    assert np.all((t[:, 9] > 0.3) & (t[:, 9] < 1.0)) and np.all(np.diff(t[:, 9]) < 0)
     # a console line every 1000 observations (1500 per density)
     assert sum(1 for line in r.stdout.splitlines() if line.split()[:1] and line.split()[0] in ("0.1", "0.2", "0.3")) == 3
 
@@ -127,7 +128,9 @@ def test_run_fluctuations_driver(ljlib, tmp_path, ensemble):
     assert np.all(gr[r < 0.8] < 1e-3)                               # hard core
     far = (r > 2.5) & (r < 3.5)
     assert abs(gr[far].mean() - 1.0) < 0.15                         # g(r) -> 1
-    assert 1.2 < gr.max() < 4.0                                     # first shell
+    # first shell; the last bin collects every pair beyond its edge (the GPU
+    # clamp rule of the reference, MDSystem.cu:39), as in the reference's output
+    assert 1.2 < gr[:-1].max() < 4.0 and gr[-1] > 10
     for ax in "XYZ":
         f = _table(base + ".flucs%s.dat" % ax)
         assert f.shape == (19, 6)
@@ -137,5 +140,5 @@ def test_run_fluctuations_driver(ljlib, tmp_path, ensemble):
     assert cube.shape == (19, 6) and np.all(np.diff(cube[:, 1]) > 0)
     vz = _table(base + ".flucsVz.dat")
     assert vz.shape == (20, 7)
-    assert np.allclose(vz[:, 0], np.sqrt(1.4) * 3 * 0.05 * np.arange(1, 21), rtol=1e-9)
-    assert np.all(np.diff(vz[:, 1]) >= 0) and vz[-1, 2] > 0.98         # nearly all |v_z| < 3 sqrt(T)
+    assert np.allclose(vz[:, 0], np.sqrt(1.4) * 3 * 0.05 * np.arange(1, 21), rtol=1e-5)  # 6 printed digits
+    assert np.all(np.diff(vz[:, 1]) >= 0) and vz[-1, 2] > 0.95         # nearly all |v_z| < 3 sqrt(T*)
