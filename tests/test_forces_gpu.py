@@ -2,7 +2,7 @@
 
 Every case goes through the C ABI (ljgb -> liblj_gb300.so) and is compared
 with the FP64 oracle restatement on identical seeded inputs.  Gate of the
-mixed-precision path (written here, stated in the spec terms): for
+mixed-precision path (written here, in the terms of the 1e-5 accuracy target): for
 every particle |dF_i| <= 1e-5 * max(|F_i|, rms|F|) -- relative to its own
 force, or to the rms force for particles whose force nearly cancels (where
 |dF_i|/|F_i| is ill-conditioned) -- and the median of |dF_i|/|F_i| <= 1e-5;
