@@ -194,7 +194,10 @@ bool ensure_ctx(int n, int block_hint) {
   REF_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   REF_CHECK(pair_occupancy(0, shape, &per_sm));
   Schedule s;
-  if (!build_schedule(&n, 1, kShapes[shape].threads, kShapes[shape].tile, sms * per_sm, 8, &s)) {
+  // at most 8 CTAs per i-block (a block's epilogue sums one segment per CTA)
+  const int nb_i = (n + kShapes[shape].threads - 1) / kShapes[shape].threads;
+  const int ctas = std::min(sms * per_sm, 8 * nb_i);
+  if (!build_schedule(&n, 1, kShapes[shape].threads, kShapes[shape].tile, ctas, 8, &s)) {
     g_status = LJ_ERR_INVALID;
     g_error = "cannot build the pair schedule";
     return false;

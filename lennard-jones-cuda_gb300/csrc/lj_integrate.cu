@@ -392,9 +392,9 @@ __global__ void k_tvn_close(StateArgs s) {
     for (int c = 0; c < 3; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
     if (B == s.sys_block_first[bi.sys]) {
       sc.Tkin_rec = sc.Tkin;
-      sc.obs_pending = 1;
+      sc.obs_slot = 0;
+      sc.obs_pending = MODE_TVN;
     }
-    if (B == 0) s.glob_cnt[1] = 0;  // ticket counter of the next pair kernel's pending_observables
   }
 }
 

@@ -33,13 +33,15 @@ struct DevScalars {
   int status;
   int rec_cap;
   long long rec_count;
-  // Fused TVN steps compute a step's observables late (inside the next
-  // step's pair kernel, or in k_obs_finalize): obs_pending marks a box whose
-  // K/V/W block partials are written but not yet summed; Tkin_rec is the
-  // Tkin of that step for its record.
+  // Fused steps compute a step's observables late (inside the next step's
+  // pair kernel, or in k_obs_finalize): obs_pending is the step mode
+  // (MODE_EVN / MODE_TVN) of a box whose K/V/W block partials are written
+  // but not yet summed, 0 if none; obs_slot is the first of the three
+  // block-partial slots that hold them; Tkin_rec is the Tkin of that step
+  // for its record.
   double Tkin_rec;
   int obs_pending;
-  int pad_;
+  int obs_slot;
 };
 
 // Observable record layout written by the device (matches lj_observables).

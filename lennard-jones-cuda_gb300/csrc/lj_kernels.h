@@ -84,9 +84,11 @@ struct StateArgs {
   int* status;
   int4* q_next;                // fused step: predictor shadow for the next step
   int* blk_cnt;                // fused step: segments finished per i-block
-  int* glob_cnt;               // fused step: [0] blocks finished, [1] pending-observables tickets
+  int* glob_cnt;               // fused step: [0] blocks finished, [2 + parity] pending-observables tickets
   int nblocks;                 // i-blocks of all boxes
   int nsys;                    // boxes
+  int obs_slot;                // fused EVN: first block-partial slot of this step's K, V, W (0 or 4, by parity)
+  int ticket;                  // fused: glob_cnt index of this step's pending-observables tickets (2 or 3)
 };
 
 enum StepMode { MODE_FORCES_ONLY = 0, MODE_EVN = 1, MODE_TVN = 2 };

@@ -184,6 +184,7 @@ void plan_static(int n, int ctas, StaticPlan* s) {
   const int nb = (n + kBI - 1) / kBI, njt = (n + kTile - 1) / kTile;
   const int ntiles = nb * njt;
   int G = ctas < ntiles ? ctas : ntiles;
+  if (G > 8 * nb) G = 8 * nb;  // at most 8 CTAs (segments) per i-block
   if (G > kMaxCtas) G = kMaxCtas;
   constexpr int kOverhead = 8;
   auto cost_before = [&](int t) -> long long {  // tiles are equal-cost except the ragged last of each block

@@ -183,6 +183,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
 
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
+  if (EPI && g == 0 && tid == 0) st.glob_cnt[st.ticket ^ 1] = 0;  // the other parity's ticket counter
   // This CTA's j range: from offset lo0 of its first tile to offset lo1 of
   // tile t1 (lo1 = 0: up to the end of tile t1 - 1).
   const int t0 = a.cta_tile_begin[g], t1 = a.cta_tile_begin[g + 1];
@@ -375,9 +376,14 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           __syncthreads();
           if (sflag) {
             __threadfence();
-            for (int sys = 0; sys < st.nsys; ++sys) {
-              if (EPI == MODE_EVN) observables_box<MODE_EVN>(st, sys, shd);
-              else tvn_chi_box(st, sys, shd);
+            if (EPI == MODE_EVN) {
+              // the observables of this step are summed later (pending_observables)
+              for (int sys = tid; sys < st.nsys; sys += THREADS) {
+                st.sc[sys].obs_slot = st.obs_slot;
+                st.sc[sys].obs_pending = MODE_EVN;
+              }
+            } else {
+              for (int sys = 0; sys < st.nsys; ++sys) tvn_chi_box(st, sys, shd);
             }
             if (tid == 0) st.glob_cnt[0] = 0;
           }
@@ -399,18 +405,20 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     }
   }
 
-  if (EPI == MODE_TVN) {
+  if (EPI) {
     // This CTA's pair work is done: the first CTAs to get here compute the
-    // observables the previous step's k_tvn_close left pending (one box per
-    // ticket), in time the SM would otherwise leave to the CTAs still busy.
+    // observables the previous step left pending (one box per ticket), in
+    // time the SM would otherwise leave to the CTAs still busy.  The ticket
+    // counters alternate by step parity; CTA 0 clears the other one at its
+    // start, after the previous step's kernels have completed.
     __shared__ int ticket;
     __syncthreads();
-    if (tid == 0) ticket = atomicAdd(st.glob_cnt + 1, 1);
+    if (tid == 0) ticket = atomicAdd(st.glob_cnt + st.ticket, 1);
     __syncthreads();
     if (ticket < st.nsys && !sfail) pending_observables(st, ticket, gridDim.x, shd);
     // The dependent kernel of a fused TVN step (k_tvn_close) may be scheduled
     // from here on; it waits for this grid's completion before reading.
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (EPI == MODE_TVN) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   }
   __syncthreads();
   if (sfail) {

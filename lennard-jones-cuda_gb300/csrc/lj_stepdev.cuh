@@ -61,10 +61,11 @@ __device__ __forceinline__ double box_sum(const StateArgs& s, int b0, int b1, in
 
 // Sums of blk_part[b][0..2] (K, V, W) over the blocks of one box in one
 // block reduction (fixed order); valid in thread 0.  sh: 3 x 32 doubles.
-__device__ __forceinline__ void box_sum3(const StateArgs& s, int b0, int b1, double* sh, double (&out)[3]) {
+__device__ __forceinline__ void box_sum3(const StateArgs& s, int b0, int b1, double* sh, double (&out)[3],
+                                         int slot = 0) {
   double acc[3] = {0.0, 0.0, 0.0};
   for (int b = b0 + (int)threadIdx.x; b < b1; b += blockDim.x) {
-    const double* bp = s.blk_part + (size_t)b * 8;
+    const double* bp = s.blk_part + (size_t)b * 8 + slot;
     acc[0] += __ldcg(bp);
     acc[1] += __ldcg(bp + 1);
     acc[2] += __ldcg(bp + 2);
@@ -79,11 +80,11 @@ __device__ __forceinline__ void box_sum3(const StateArgs& s, int b0, int b1, dou
 // steps (MDSystem.cpp:582) and the optional per-step record.  Block-wide call;
 // thread 0 writes.  sh: 3 x 32 doubles.
 template <int MODE>
-__device__ __forceinline__ void observables_box(const StateArgs& s, int sys, double* sh) {
+__device__ __forceinline__ void observables_box(const StateArgs& s, int sys, double* sh, int slot = 0) {
   const BoxArgs box = s.boxes[sys];
   const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
   double kvw[3];
-  box_sum3(s, b0, b1, sh, kvw);
+  box_sum3(s, b0, b1, sh, kvw, slot);
   const double K = kvw[0], V = kvw[1], W = kvw[2];
   if (threadIdx.x != 0) return;
   DevScalars& sc = s.sc[sys];
@@ -127,18 +128,21 @@ __device__ __forceinline__ void observables_box(const StateArgs& s, int sys, dou
   }
 }
 
-// Observables of the boxes whose fused TVN step left them pending (block
-// partials K, V, W written by k_tvn_close).  Called with a ticket from
-// 0 .. tickets-1; ticket k takes boxes k, k + tickets, ...  Block-wide call.
+// Observables of the boxes whose fused step left them pending (block
+// partials K, V, W from k_tvn_close or the EVN epilogues, at obs_slot).
+// Called with a ticket from 0 .. tickets-1; ticket k takes boxes k,
+// k + tickets, ...  Block-wide call.
 static __device__ __noinline__ void pending_observables(const StateArgs& s, int ticket, int tickets, double* sh) {
-  __shared__ int pend;
+  __shared__ int pend, slot;
   for (int sys = ticket; sys < s.nsys; sys += tickets) {
-    if (threadIdx.x == 0) pend = s.sc[sys].obs_pending;
-    __syncthreads();
-    if (pend) {
-      observables_box<MODE_TVN>(s, sys, sh);
-      if (threadIdx.x == 0) s.sc[sys].obs_pending = 0;
+    if (threadIdx.x == 0) {
+      pend = s.sc[sys].obs_pending;
+      slot = s.sc[sys].obs_slot;
     }
+    __syncthreads();
+    if (pend == MODE_TVN) observables_box<MODE_TVN>(s, sys, sh, slot);
+    else if (pend == MODE_EVN) observables_box<MODE_EVN>(s, sys, sh, slot);
+    if (pend && threadIdx.x == 0) s.sc[sys].obs_pending = 0;
     __syncthreads();
   }
 }
@@ -182,7 +186,9 @@ __device__ __forceinline__ void segment_sums(const StateArgs& s, const BlockInfo
 // the predictor written by the previous step.
 //   EVN (MDSystem.cpp:443-463): x_{n+1}; v_{n+1} = v_n + dt F_n/2 +
 //       dt F_{n+1}/2; boundaries; the predictor of the next step into
-//       q_next.  Block partials [0] K, [1] V, [2] W.
+//       q_next.  Block partials K, V, W at obs_slot .. obs_slot + 2 (the
+//       slots alternate by step parity: the next step's epilogues write
+//       while its first-finishing CTAs read this step's).
 //   TVN (MDSystem.cpp:469-497): only what chi needs before any velocity can
 //       be set -- F_{n+1} (kept in s.tf until k_tvn_close moves it to s.f),
 //       e, w, and the half-kicked velocity's sum of squares in partial [3].
@@ -252,7 +258,7 @@ __device__ __noinline__ void fused_block_step(const StateArgs& s, int B, double*
   if (tid == 0) {
     if constexpr (MODE == MODE_EVN) {
 #pragma unroll
-      for (int c = 0; c < NP; ++c) s.blk_part[(size_t)B * 8 + c] = part[c];
+      for (int c = 0; c < NP; ++c) s.blk_part[(size_t)B * 8 + s.obs_slot + c] = part[c];
     } else {
       s.blk_part[(size_t)B * 8 + 3] = part[0];
     }

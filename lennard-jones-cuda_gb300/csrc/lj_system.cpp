@@ -30,6 +30,7 @@ thread_local std::string g_create_error;
 // Tile overhead in j-record units (barrier, compensation, refill) used to
 // weight ragged tiles in the stream-K split.
 constexpr int kTileOverhead = 8;
+constexpr int kMaxSegmentsPerBlock = 8;
 
 template <typename T>
 struct DevBuf {
@@ -83,7 +84,7 @@ struct lj_system {
   DevBuf<double4_32a> xd;
   DevBuf<int> blk_cnt, glob_cnt;  // fused-step completion counters
   int qpar = 0;             // which of q / q2 holds the current shadow
-  bool obs_maybe_pending = false;  // a fused TVN step left observables pending (DevScalars::obs_pending)
+  bool obs_maybe_pending = false;  // a fused step left observables pending (DevScalars::obs_pending)
   bool pred_ready = false;  // current shadow = predictor x + dt v + dt^2 F/2 for pred_dt
   double pred_dt = 0.0;
   DevBuf<BlockInfo> blocks;
@@ -178,6 +179,8 @@ StateArgs state_args(lj_system* s) {
   a.glob_cnt = s->glob_cnt.p;
   a.nblocks = (int)s->sched.blocks.size();
   a.nsys = s->nsys;
+  a.obs_slot = 4 * s->qpar;
+  a.ticket = 2 + s->qpar;
   return a;
 }
 
@@ -272,8 +275,16 @@ lj_status setup_schedule(lj_system* s) {
   if (blocks_per_sm < 1) return fail(s, LJ_ERR_NO_DEVICE, "pair kernel cannot be resident on this device");
   std::vector<int> n(s->nsys);
   for (int k = 0; k < s->nsys; ++k) n[k] = s->cfg[k].n;
+  // At most kMaxSegmentsPerBlock CTAs per i-block: a small box spread over
+  // the whole persistent grid leaves each block dozens of partial segments,
+  // and the block epilogue that sums them serially becomes the step's tail
+  // (N=2048 EVN: 34.1 -> 25.8 us per step with 8; N >= 8 x 128 x SMs x
+  // occupancy / 128 is unaffected).
+  long long nbt = 0;
+  for (int k = 0; k < s->nsys; ++k) nbt += (n[k] + threads - 1) / threads;
+  const int G = (int)std::min<long long>((long long)s->num_sms * blocks_per_sm, nbt * kMaxSegmentsPerBlock);
   Schedule sch;
-  if (!build_schedule(n.data(), s->nsys, threads, tile, s->num_sms * blocks_per_sm, kTileOverhead, &sch))
+  if (!build_schedule(n.data(), s->nsys, threads, tile, G, kTileOverhead, &sch))
     return fail(s, LJ_ERR_INVALID, "cannot build the pair schedule");
   s->sched = std::move(sch);
   s->BI = threads;
@@ -286,9 +297,9 @@ lj_status setup_schedule(lj_system* s) {
   LJ_CUDA(s, s->sys_block_first.alloc(s->nsys + 1));
   LJ_CUDA(s, s->blk_part.alloc((size_t)nb * 8));
   LJ_CUDA(s, s->blk_cnt.alloc(nb));
-  LJ_CUDA(s, s->glob_cnt.alloc(2));
+  LJ_CUDA(s, s->glob_cnt.alloc(4));
   LJ_CUDA(s, cudaMemsetAsync(s->blk_cnt.p, 0, sizeof(int) * nb, s->stream));
-  LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * 2, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * 4, s->stream));
   s->pred_ready = false;
   // partial: nseg x 5 x BI values of 8 bytes (FP64) or 4 bytes (MIXED)
   const size_t vals = (size_t)s->sched.nseg * 5 * threads;
@@ -530,7 +541,7 @@ lj_status check_status(lj_system* s) {
     LJ_CUDA(s, cudaMemset(s->status.p, 0, sizeof(int)));
     // A failed launch may leave the fused-step counters mid-count.
     if (s->blk_cnt.p) LJ_CUDA(s, cudaMemset(s->blk_cnt.p, 0, sizeof(int) * s->blk_cnt.n));
-    if (s->glob_cnt.p) LJ_CUDA(s, cudaMemset(s->glob_cnt.p, 0, sizeof(int) * 2));
+    if (s->glob_cnt.p) LJ_CUDA(s, cudaMemset(s->glob_cnt.p, 0, sizeof(int) * 4));
     s->pred_ready = false;
     if (st & LJ_DEVFLAG_TIMEOUT)
       return fail(s, LJ_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the results of that launch are void");
@@ -880,7 +891,7 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
   }
   const int mode = step_mode(s);
   const bool fused = use_fused(s);
-  if (!fused || mode != MODE_TVN) {
+  if (!fused) {
     lj_status st = flush_observables(s);
     if (st) return st;
   }
@@ -904,7 +915,7 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
     LJ_CUDA(s, cudaGraphLaunch(ge->exec, s->stream));
     s->launches += ge->kernels;
     if (fused) s->qpar ^= 1;  // the step wrote the next predictor into the other buffer
-    if (fused && mode == MODE_TVN) s->obs_maybe_pending = true;
+    if (fused) s->obs_maybe_pending = true;
     if (s->counter_cap > 0 || s->rdf_acc) {
       lj_status ast = after_step(s);
       if (ast) return ast;
@@ -1364,6 +1375,8 @@ lj_status lj_autotune(lj_system* s) {
     if (s->rec_cap > 0)
       LJ_CUDA(s, cudaMemcpyAsync(s->records.p, snap_rec.p, sizeof(DevRecord) * s->records.n,
                                  cudaMemcpyDeviceToDevice, s->stream));
+    // the fused steps' ticket counters follow the step parity restored here
+    LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * 4, s->stream));
     LJ_CUDA(s, cudaStreamSynchronize(s->stream));
     s->qpar = qpar;
     return LJ_OK;
