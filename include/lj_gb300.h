@@ -296,6 +296,16 @@ lj_status lj_rdf_accumulate(lj_system* sys, int32_t enable, int32_t mode, int32_
 /* The summed counts and the number of steps summed; reset != 0 clears both. */
 lj_status lj_rdf_accumulated(lj_system* sys, uint64_t* counts, int64_t* nsamples, int32_t reset);
 
+/* ---- Headless particle image ---------------------------------------------
+ * Stand-in for the reference's OpenGL viewer (src/gui/MDSystemGL.cpp:32-160,
+ * orange spheres of radius 0.5 sigma): a GPU splat of box `box` viewed along
+ * `axis` (0/1/2, viewer on its positive side) into width x height RGBA8
+ * pixels (host buffer, 4 bytes per pixel, row 0 at the top), spheres of
+ * `radius` sigma shaded by their view-facing normal, background black.  No
+ * graphics API is involved. */
+lj_status lj_render(lj_system* sys, int32_t box, int32_t axis, int32_t width, int32_t height, double radius,
+                    uint8_t* rgba);
+
 /* ---- Differentiable MD (adjoint) ----------------------------------------
  * No counterpart in the reference (its dynamics are not differentiable).
  * Gradients of a time-averaged trajectory loss

@@ -113,6 +113,10 @@ cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t
 cudaError_t launch_tvn_close(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
 cudaError_t launch_obs_finalize(const StateArgs& s, int nsys, cudaStream_t st);
 
+// Headless particle image (lj_render.cu): splat + shade into rgba (device).
+cudaError_t launch_render(const double* x, int npad, int p0, int n, int axis, int W, int H, double L, double R,
+                          unsigned long long* key, uint8_t* rgba, cudaStream_t st);
+
 // Subsystem counters of the fluctuation runs (lj_counters_configure).
 constexpr int kMaxCounterAlphas = 64;
 struct CounterDev {

@@ -1305,6 +1305,37 @@ lj_status lj_rdf_accumulated(lj_system* s, uint64_t* counts, int64_t* nsamples, 
   return LJ_OK;
 }
 
+lj_status lj_render(lj_system* s, int32_t box, int32_t axis, int32_t width, int32_t height, double radius,
+                    uint8_t* rgba) {
+  if (!s || !rgba) return LJ_ERR_INVALID;
+  if (box < 0 || box >= s->nsys) return fail(s, LJ_ERR_INVALID, "box %d out of range", box);
+  if (axis < 0 || axis > 2) return fail(s, LJ_ERR_INVALID, "axis must be 0, 1 or 2");
+  if (width < 1 || height < 1 || (long long)width * height > (1ll << 26))
+    return fail(s, LJ_ERR_INVALID, "image size must be 1 .. 2^26 pixels");
+  if (!(radius > 0)) return fail(s, LJ_ERR_INVALID, "radius must be > 0");
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);
+  if (st) return st;
+  const size_t npix = (size_t)width * height;
+  unsigned long long* key = nullptr;
+  uint8_t* img = nullptr;
+  LJ_CUDA(s, cudaMalloc(&key, sizeof(unsigned long long) * npix));
+  cudaError_t e = cudaMalloc(&img, 4 * npix);
+  if (e == cudaSuccess) {
+    int p0 = 0;
+    for (int k = 0; k < box; ++k) p0 += s->cfg[k].n;
+    e = launch_render(s->x.p, s->npad, p0, s->cfg[box].n, axis, width, height, s->boxes[box].L,
+                      radius * s->cfg[box].sigma, key, img, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rgba, img, 4 * npix, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    s->launches += 2;
+  }
+  cudaFree(key);
+  if (img) cudaFree(img);
+  LJ_CUDA(s, e);
+  return LJ_OK;
+}
+
 lj_status lj_tune_info(lj_system* s, int32_t* nshapes, int32_t* active, int32_t k, int32_t* threads, int32_t* ipt,
                        int32_t* tile) {
   if (!s) return LJ_ERR_INVALID;

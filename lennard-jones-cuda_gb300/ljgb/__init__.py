@@ -126,6 +126,7 @@ def _declare(L):
         "lj_counters_read": (C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_int32)]),
         "lj_rdf_accumulate": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
         "lj_rdf_accumulated": (C.c_int, [_P, _P, C.POINTER(C.c_int64), C.c_int32]),
+        "lj_render": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, _P]),
         "lj_adjoint_create": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(_P)]),
         "lj_adjoint_destroy": (C.c_int, [_P]),
         "lj_adjoint_last_error": (C.c_char_p, [_P]),
@@ -212,6 +213,15 @@ def pinned(shape, dtype=np.float64) -> np.ndarray:
 
 def reference_rdf_dr2(n: int) -> float:
     return float(load().lj_reference_rdf_dr2(int(n)))
+
+
+def write_ppm(path: str, rgba) -> None:
+    """Writes an RGBA image (System.render) as a binary PPM (P6) file."""
+    rgba = np.asarray(rgba, np.uint8)
+    h, w = rgba.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(rgba[:, :, :3]).tobytes())
 
 
 def sample_initial_state(cfg: Config):
@@ -406,6 +416,12 @@ class System:
         n = C.c_int64()
         self._c(load().lj_rdf_accumulated(self.h, out.ctypes.data, C.byref(n), int(bool(reset))))
         return out, n.value
+
+    def render(self, box: int = 0, axis: int = 2, width: int = 512, height: int = 512, radius: float = 0.5):
+        """Headless particle image (lj_render): (height, width, 4) uint8 RGBA."""
+        img = np.zeros((height, width, 4), np.uint8)
+        self._c(load().lj_render(self.h, box, axis, width, height, radius, img.ctypes.data))
+        return img
 
     def set_kernel_shape(self, shape: int):
         self._c(load().lj_set_kernel_shape(self.h, int(shape)))

@@ -27,6 +27,7 @@ SOURCES = [
     "lj_compat.cu",
     "lj_noalloc.cu",
     "lj_adjoint.cu",
+    "lj_render.cu",
     "lj_system.cpp",
     "lj_schedule.cpp",
     "lj_init.cpp",

@@ -142,3 +142,20 @@ def test_run_fluctuations_driver(ljlib, tmp_path, ensemble):
     assert vz.shape == (20, 7)
     assert np.allclose(vz[:, 0], np.sqrt(1.4) * 3 * 0.05 * np.arange(1, 21), rtol=1e-5)  # 6 printed digits
     assert np.all(np.diff(vz[:, 1]) >= 0) and vz[-1, 2] > 0.95         # nearly all |v_z| < 3 sqrt(T*)
+
+
+@pytest.mark.parametrize("axis,W,H", [(2, 96, 96), (0, 80, 64)])
+def test_headless_render_matches_restatement(ljgb_mod, axis, W, H):
+    """The GPU splat image is pixel-identical to the CPU restatement of the
+    same rules (oracle/render.py) on the same positions."""
+    import render
+    s = ljgb_mod.System(n=200, density=0.3, temperature=1.0, lattice=ljgb_mod.LATTICE_FCC, jitter=0.05)
+    s.integrate(0.005, 20)
+    p, _, _ = s.get_state()
+    img = s.render(0, axis, W, H, 0.5)
+    want = render.render(p, s.L, axis, W, H, 0.5)
+    assert img.shape == (H, W, 4)
+    assert np.array_equal(img, want)
+    lit = (img[:, :, 0] > 0).mean()
+    assert 0.2 < lit < 1.0                              # particles cover part of the view
+    assert set(np.unique(img[:, :, 2])) == {0}          # orange: no blue channel
