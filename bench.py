@@ -335,6 +335,20 @@ def extra_configs(torch, ljgb, oracle, dev, flush, peak):
     return out
 
 
+def max_over_ranks(ms: float, device: str) -> float:
+    """The slowest rank's timed region (every rank calls this)."""
+    import torch
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, pairs_per_step: int, steps: int, total_ms: float) -> float:
+    """Whole-job pair-interactions/s: every rank runs its own box (replicas,
+    weak scaling) and the job takes as long as the slowest rank."""
+    return world * pairs_per_step * steps / (total_ms * 1e-3)
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import ljgb
@@ -358,11 +372,9 @@ def gpu_arm(args, rank, world, local_rank):
         total_ms, per_step, launches = timed_steps(torch, s, args.steps, args.warmup, flush)
     torch.cuda.synchronize()
     if dist:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, "cuda")
     pairs_step = N * (N - 1)
-    value = world * pairs_step * args.steps / (total_ms * 1e-3)
+    value = replica_value(world, pairs_step, args.steps, total_ms)
     ms_step = total_ms / args.steps
 
     # pair-kernel duration inside the same step graph (event nodes around it)

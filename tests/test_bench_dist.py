@@ -1,0 +1,58 @@
+"""The multi-GPU (replica) logic of bench.py on CPU: two gloo ranks agree on
+the slowest rank's time, the whole-job value counts every rank's box, and the
+reference arm runs on rank 0 only."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.multiprocessing as mp  # noqa: E402
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, out):
+    import sys
+    sys.path.insert(0, REPO)
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    local_ms = [120.0, 250.0][rank]
+    slowest = bench.max_over_ranks(local_ms, "cpu")
+    value = bench.replica_value(world, 16384 * 16383, 200, slowest)
+    torch.distributed.barrier()
+    torch.distributed.destroy_process_group()
+    out.put((rank, slowest, value))
+
+
+def test_two_rank_max_and_value():
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in range(world))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [r[1] for r in res] == [250.0, 250.0]
+    assert res[0][2] == res[1][2] == pytest.approx(2 * 16384 * 16383 * 200 / 0.250)
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    import sys
+    sys.path.insert(0, REPO)
+    import bench
+
+    class A:
+        steps, warmup = 1, 1
+    assert bench.reference_arm(A(), rank=1, world=2) is None
