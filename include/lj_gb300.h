@@ -42,7 +42,10 @@ typedef enum {
   LJ_ERR_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up; results of that launch are void */
   LJ_ERR_NONFINITE = 5,   /* an observable became NaN/Inf (overlapping particles, blow-up) */
   LJ_ERR_UNSUPPORTED = 6, /* requested mode is not provided (e.g. the CPU hardware mode) */
-  LJ_ERR_OUT_OF_MEMORY = 7
+  LJ_ERR_OUT_OF_MEMORY = 7,
+  LJ_ERR_ESCAPED = 8      /* a particle of a hard-wall box went more than max(sigma, L/20) beyond
+                             the walls and its starting bounding box (blow-up); no counterpart in
+                             the reference, whose walls have no frame to leave */
 } lj_status;
 
 /* Boundary conditions, MDSystem.h:24: 0 periodic, 1 hard wall, 2 none. */
@@ -285,7 +288,13 @@ typedef struct {
 /* Enables the counters (ncounters = 0 disables them); ring_steps rows are
  * kept between reads. */
 lj_status lj_counters_configure(lj_system* sys, const lj_counter* counters, int32_t ncounters, int32_t ring_steps);
-/* Copies the rows of the steps since the last read, oldest first: per step
+/* Counts after every `every`-th step only (default 1; kept across
+ * lj_counters_configure calls), counted from this call or the last
+ * configure: the semi-grand-canonical task of the reference
+ * (src/tasks/semiGCEfluctuations/semiGCEfluctuations.cpp:70-80) samples every
+ * 200 steps. */
+lj_status lj_counters_set_interval(lj_system* sys, int32_t every);
+/* Copies the rows of the counted steps since the last read, oldest first: per step
  * and counter, the cumulative counts N(alpha_0) .. N(alpha_{nalpha-1}).  With
  * counts = NULL only *nsteps is set.  More steps than ring_steps since the
  * last read is an error (LJ_ERR_INVALID) and drops them. */

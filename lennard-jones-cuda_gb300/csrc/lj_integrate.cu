@@ -24,7 +24,8 @@ namespace {
 constexpr int kObsThreads = 256;
 
 __device__ __forceinline__ void store_shadow(const StateArgs& s, const DevScalars& sc, int p, double x,
-                                             double y, double z) {
+                                             double y, double z, const BoxArgs& box) {
+  check_wall_frame(s, box.bc, sc, x, y, z);
   int4 q;
   q.x = fixed_coord(x, sc.origin[0], sc.invP);
   q.y = fixed_coord(y, sc.origin[1], sc.invP);
@@ -101,7 +102,7 @@ __global__ void k_drift(StateArgs s) {
       if (MODE == MODE_EVN) s.v[k] = fma(box.hdt, f, v[c]);
       if (MODE == MODE_TVN) s.tf[k] = 0.5 * f;
     }
-    if (box.bc == 0) store_shadow(s, s.sc[bi.sys], p, x[0], x[1], x[2]);
+    if (box.bc == 0) store_shadow(s, s.sc[bi.sys], p, x[0], x[1], x[2], box);
   }
   if (box.bc != 0) block_bbox(s, B, valid, x, sh);
 }
@@ -120,9 +121,20 @@ __global__ void k_bbox(StateArgs s) {
   block_bbox(s, B, valid, x, sh);
 }
 
-// Fixed-point frame per box.  Periodic: origin 0, period L.  Walls / open:
-// origin at the bounding-box minimum, period 2.002 x the largest extent (so
-// no pair separation wraps).  Also the FP32 scale constants of the pair kernel.
+// Fixed-point frame per box: origin and period P such that every position
+// maps into [0, P/2) (no pair separation wraps), except for periodic boxes.
+// Also the FP32 scale constants of the pair kernel.
+//   periodic: origin 0, period L (the wrap is the minimum image);
+//   walls:    the bounding box of the positions joined with [0, L], widened
+//             by m = max(sigma, L/20) on every side, P = 2.002 x its largest
+//             extent.  A wall turns a particle back within a step or two of
+//             crossing it, so the frame stays valid while the fused step
+//             keeps it fixed; a position outside it sets LJ_DEVFLAG_ESCAPED
+//             (check_wall_frame, wherever a shadow is written);
+//   open:     origin at the bounding-box minimum, P = 2.002 x the largest
+//             extent, recomputed after every drift.
+// The bounding box comes from the block partials blk_part[b][0..5]
+// (k_bbox, or k_drift of the kernel-per-phase step).
 __global__ void k_frame(StateArgs s, int only_nonperiodic) {
   __shared__ double sh[32];
   const int sys = blockIdx.x;
@@ -157,6 +169,10 @@ __global__ void k_frame(StateArgs s, int only_nonperiodic) {
         a = fmin(a, sh[w]);
         b = fmax(b, sh[16 + w]);
       }
+      if (box.bc == 1) {
+        a = fmin(a, 0.0) - box.wall_margin;
+        b = fmax(b, box.L) + box.wall_margin;
+      }
       lo[c] = a;
       hi[c] = b;
     }
@@ -184,7 +200,7 @@ __global__ void k_quantize(StateArgs s, int only_nonperiodic) {
   if (only_nonperiodic && s.boxes[bi.sys].bc == 0) return;
   if ((int)threadIdx.x >= bi.n_i) return;
   const int p = bi.p0 + bi.i0 + threadIdx.x;
-  store_shadow(s, s.sc[bi.sys], p, s.x[p], s.x[(size_t)s.npad + p], s.x[2 * (size_t)s.npad + p]);
+  store_shadow(s, s.sc[bi.sys], p, s.x[p], s.x[(size_t)s.npad + p], s.x[2 * (size_t)s.npad + p], s.boxes[bi.sys]);
 }
 
 // ---------------------------------------------------------------------------
@@ -320,7 +336,7 @@ __global__ void k_observables(StateArgs s) {
 }
 
 // Predictor of the fused step: the shadow of x + dt v + dt^2 F / 2 (the
-// positions the next pair kernel evaluates), periodic boxes.
+// positions the next pair kernel evaluates), periodic and walled boxes.
 __global__ void k_predict(StateArgs s) {
   const BlockInfo bi = s.blocks[blockIdx.x];
   if ((int)threadIdx.x >= bi.n_i) return;
@@ -332,7 +348,9 @@ __global__ void k_predict(StateArgs s) {
     const size_t k = (size_t)c * s.npad + p;
     xp[c] = drift_pos(box, s.x[k], s.v[k], s.f[k]);
   }
-  s.q[p] = shadow_of(s.sc[bi.sys], xp[0], xp[1], xp[2]);
+  const DevScalars& sc = s.sc[bi.sys];
+  check_wall_frame(s, box.bc, sc, xp[0], xp[1], xp[2]);
+  s.q[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
 }
 
 // Close of a fused TVN step (MDSystem.cpp:469-506, :578-579).  The pair
@@ -381,6 +399,7 @@ __global__ void k_tvn_close(StateArgs s) {
       s.f[k] = f1[c];
       xp[c] = drift_pos(box, x[c], v[c], f1[c]);
     }
+    check_wall_frame(s, box.bc, sc, xp[0], xp[1], xp[2]);
     s.q_next[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
     part[0] = 0.5 * fma(v[0], v[0], fma(v[1], v[1], v[2] * v[2]));
     part[1] = 0.5 * s.e[p];

@@ -9,6 +9,7 @@ namespace ljgb {
 enum : int {
   LJ_DEVFLAG_TIMEOUT = 1,    // a bounded mbarrier wait gave up
   LJ_DEVFLAG_NONFINITE = 2,  // NaN/Inf observable
+  LJ_DEVFLAG_ESCAPED = 4,    // a particle of a walled box left its fixed frame
 };
 
 // Per-system frame of the fixed-point shadow and the scalar state that the
@@ -83,6 +84,7 @@ struct BoxArgs {
   double kP;     // rho / N:    P = (W / 6 + N T) kP
   double inv3N;  // 1 / (3 N):  Tkin = inv3N sum tv^2
   double invT0;  // 1 / T0 (0 when T0 = 0)
+  double wall_margin;  // walls: m = max(sigma, L / 20), the frame's margin beyond [0, L] and the positions
 };
 
 }  // namespace ljgb

@@ -368,24 +368,29 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           __threadfence();
           fused_block_step<EPI>(st, B, shd);
           __syncthreads();
+          // Last block of its box?  That CTA finishes the box: EVN marks its
+          // observables pending (summed later by pending_observables), TVN
+          // computes its chi.  Boxes finish independently, so a batch of
+          // many boxes has no serial stage at the end of the grid.
+          const int sys = bi.sys;
           if (tid == 0) {
             st.blk_cnt[B] = 0;
             __threadfence();
-            sflag = (atomicAdd(st.glob_cnt, 1) == st.nblocks - 1);
+            const int nb_box = st.sys_block_first[sys + 1] - st.sys_block_first[sys];
+            sflag = (atomicAdd(st.glob_cnt + 4 + sys, 1) == nb_box - 1);
           }
           __syncthreads();
           if (sflag) {
             __threadfence();
             if (EPI == MODE_EVN) {
-              // the observables of this step are summed later (pending_observables)
-              for (int sys = tid; sys < st.nsys; sys += THREADS) {
+              if (tid == 0) {
                 st.sc[sys].obs_slot = st.obs_slot;
                 st.sc[sys].obs_pending = MODE_EVN;
               }
             } else {
-              for (int sys = 0; sys < st.nsys; ++sys) tvn_chi_box(st, sys, shd);
+              tvn_chi_box(st, sys, shd);
             }
-            if (tid == 0) st.glob_cnt[0] = 0;
+            if (tid == 0) st.glob_cnt[4 + sys] = 0;
           }
           __syncthreads();
         }

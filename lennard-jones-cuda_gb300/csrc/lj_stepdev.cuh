@@ -45,6 +45,20 @@ __device__ __forceinline__ double tvn_chi(const BoxArgs& b, double tv2, double* 
   return b.T0 > 0 ? rsqrt(Tkin * b.invT0) : sqrt(b.T0 / Tkin);
 }
 
+// Walled boxes keep their fixed-point frame between frame updates (k_frame):
+// a position outside [0, P/2) of it could wrap in the fixed-point
+// differences, so it is flagged (the quantisation moves a coordinate by at
+// most one unit, hence the slightly smaller bound).
+__device__ __forceinline__ void check_wall_frame(const StateArgs& s, int bc, const DevScalars& sc, double x,
+                                                 double y, double z) {
+  if (bc != 1) return;
+  const double ux = (x - sc.origin[0]) * sc.invP, uy = (y - sc.origin[1]) * sc.invP,
+               uz = (z - sc.origin[2]) * sc.invP;
+  constexpr double kHi = 0.4999;
+  if (!(ux >= 0.0 && ux < kHi && uy >= 0.0 && uy < kHi && uz >= 0.0 && uz < kHi))
+    atomicOr(s.status, LJ_DEVFLAG_ESCAPED);
+}
+
 __device__ __forceinline__ int4 shadow_of(const DevScalars& sc, double x, double y, double z) {
   return make_int4(fixed_coord(x, sc.origin[0], sc.invP), fixed_coord(y, sc.origin[1], sc.invP),
                    fixed_coord(z, sc.origin[2], sc.invP), 0);
@@ -237,6 +251,7 @@ __device__ __noinline__ void fused_block_step(const StateArgs& s, int B, double*
         xp[c] = drift_pos(box, x, v, Fn1[c]);
         vv = fma(v, v, vv);
       }
+      check_wall_frame(s, box.bc, sc, xp[0], xp[1], xp[2]);
       s.q_next[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
       part[0] = 0.5 * vv;
       part[1] = 0.5 * e;

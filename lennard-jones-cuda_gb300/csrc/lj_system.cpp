@@ -70,6 +70,7 @@ struct lj_system {
   int num_sms = 0;
   int prec = LJ_PREC_MIXED;
   bool any_nonperiodic = false;
+  bool any_open = false;  // a box without walls (bc 2): its frame follows the particles
 
   // kernel shape / schedule
   int shape = 0;        // index into kShapes (MIXED)
@@ -104,6 +105,8 @@ struct lj_system {
   DevBuf<CounterDev> dcounters;
   DevBuf<int> counter_ring;
   int counter_bins = 0, counter_cap = 0;
+  int counter_every = 1;         // count after every counter_every-th step
+  long long counter_phase = 0;   // steps since the last counted one
   long long counter_head = 0, counter_tail = 0;  // rows written / rows read
   // RDF summed over steps (lj_rdf_accumulate), from its own shadow buffer
   bool rdf_acc = false;
@@ -246,6 +249,7 @@ BoxArgs box_args(const lj_config& c) {
 
 lj_status upload_boxes(lj_system* s) {
   s->any_nonperiodic = false;
+  s->any_open = false;
   for (auto& b : s->boxes) {
     s->any_nonperiodic |= (b.bc != 0);
     b.hdt = 0.5 * b.dt;
@@ -255,6 +259,8 @@ lj_status upload_boxes(lj_system* s) {
     b.kP = b.rho / b.N;
     b.inv3N = 1.0 / (3.0 * b.N);
     b.invT0 = b.T0 > 0 ? 1.0 / b.T0 : 0.0;
+    b.wall_margin = std::max(b.sigma, 0.05 * b.L);
+    s->any_open |= (b.bc == 2);
   }
   LJ_CUDA(s, cudaMemcpyAsync(s->dboxes.p, s->boxes.data(), sizeof(BoxArgs) * s->nsys, cudaMemcpyHostToDevice,
                              s->stream));
@@ -297,9 +303,9 @@ lj_status setup_schedule(lj_system* s) {
   LJ_CUDA(s, s->sys_block_first.alloc(s->nsys + 1));
   LJ_CUDA(s, s->blk_part.alloc((size_t)nb * 8));
   LJ_CUDA(s, s->blk_cnt.alloc(nb));
-  LJ_CUDA(s, s->glob_cnt.alloc(4));
+  LJ_CUDA(s, s->glob_cnt.alloc(4 + (size_t)s->nsys));
   LJ_CUDA(s, cudaMemsetAsync(s->blk_cnt.p, 0, sizeof(int) * nb, s->stream));
-  LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * 4, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n, s->stream));
   s->pred_ready = false;
   // partial: nseg x 5 x BI values of 8 bytes (FP64) or 4 bytes (MIXED)
   const size_t vals = (size_t)s->sched.nseg * 5 * threads;
@@ -408,9 +414,9 @@ lj_status enqueue_step(lj_system* s, int mode, cudaEvent_t* ev, bool capture, in
 
 // Fused step: the pair kernel carries the second half of the Verlet step in
 // the last CTA of each i-block (EVN: everything, one kernel per step; TVN: the
-// chi reduction, then k_tvn_close applies the rescale).  Needs periodic boxes
-// (constant shadow frame) and the MIXED kernel.
-bool use_fused(const lj_system* s) { return s->prec == LJ_PREC_MIXED && !s->any_nonperiodic; }
+// chi reduction, then k_tvn_close applies the rescale).  Needs a constant
+// shadow frame (periodic or walled boxes, not open ones) and the MIXED kernel.
+bool use_fused(const lj_system* s) { return s->prec == LJ_PREC_MIXED && !s->any_open; }
 
 lj_status enqueue_step_fused(lj_system* s, int mode, cudaEvent_t* ev, bool capture, int* kernels) {
   StateArgs a = state_args(s);
@@ -506,7 +512,8 @@ lj_status flush_observables(lj_system* s) {
 // Work after every step: the subsystem counters and the summed RDF, when
 // enabled (plain launches after the step's graph).
 lj_status after_step(lj_system* s) {
-  if (s->counter_cap > 0) {
+  if (s->counter_cap > 0 && ++s->counter_phase >= s->counter_every) {
+    s->counter_phase = 0;
     int* row = s->counter_ring.p + (size_t)(s->counter_head % s->counter_cap) * s->counter_bins;
     LJ_CUDA(s, cudaMemsetAsync(row, 0, sizeof(int) * s->counter_bins, s->stream));
     LJ_CUDA(s, launch_counters(state_args(s), s->dcounters.p, (int)s->counters.size(), s->counter_bins, row,
@@ -541,12 +548,16 @@ lj_status check_status(lj_system* s) {
     LJ_CUDA(s, cudaMemset(s->status.p, 0, sizeof(int)));
     // A failed launch may leave the fused-step counters mid-count.
     if (s->blk_cnt.p) LJ_CUDA(s, cudaMemset(s->blk_cnt.p, 0, sizeof(int) * s->blk_cnt.n));
-    if (s->glob_cnt.p) LJ_CUDA(s, cudaMemset(s->glob_cnt.p, 0, sizeof(int) * 4));
+    if (s->glob_cnt.p) LJ_CUDA(s, cudaMemset(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n));
     s->pred_ready = false;
     if (st & LJ_DEVFLAG_TIMEOUT)
       return fail(s, LJ_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the results of that launch are void");
     if (st & LJ_DEVFLAG_NONFINITE)
       return fail(s, LJ_ERR_NONFINITE, "an observable became NaN/Inf (overlapping particles or blow-up)");
+    if (st & LJ_DEVFLAG_ESCAPED)
+      return fail(s, LJ_ERR_ESCAPED,
+                  "a particle of a walled box went further than m = max(sigma, L/20) beyond the walls and the "
+                  "positions it started from (blow-up)");
   }
   return LJ_OK;
 }
@@ -1191,6 +1202,7 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
   s->counter_cap = 0;
   s->counter_bins = 0;
   s->counter_head = s->counter_tail = 0;
+  s->counter_phase = 0;
   if (ncounters == 0) return LJ_OK;
   if (!counters || ncounters < 0) return fail(s, LJ_ERR_INVALID, "counters must be non-NULL");
   if (ring_steps < 1) return fail(s, LJ_ERR_INVALID, "ring_steps must be >= 1");
@@ -1225,6 +1237,14 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
   return LJ_OK;
 }
 
+lj_status lj_counters_set_interval(lj_system* s, int32_t every) {
+  if (!s) return LJ_ERR_INVALID;
+  if (every < 1) return fail(s, LJ_ERR_INVALID, "the counting interval must be >= 1 step");
+  s->counter_every = every;
+  s->counter_phase = 0;
+  return LJ_OK;
+}
+
 lj_status lj_counters_read(lj_system* s, int32_t* counts, int32_t max_steps, int32_t* nsteps) {
   if (!s) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);
@@ -1240,10 +1260,13 @@ lj_status lj_counters_read(lj_system* s, int32_t* counts, int32_t max_steps, int
   if (!counts) return LJ_OK;
   const int n = (int)std::min<long long>(avail, max_steps);
   const int B = s->counter_bins;
-  for (int k = 0; k < n; ++k) {
+  // the rows are contiguous in the ring up to its end, then from its start
+  for (int k = 0; k < n;) {
     const long long row = (s->counter_tail + k) % s->counter_cap;
-    LJ_CUDA(s, cudaMemcpyAsync(counts + (size_t)k * B, s->counter_ring.p + (size_t)row * B, sizeof(int) * B,
-                               cudaMemcpyDeviceToHost, s->stream));
+    const int run = (int)std::min<long long>(n - k, s->counter_cap - row);
+    LJ_CUDA(s, cudaMemcpyAsync(counts + (size_t)k * B, s->counter_ring.p + (size_t)row * B,
+                               sizeof(int) * B * (size_t)run, cudaMemcpyDeviceToHost, s->stream));
+    k += run;
   }
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   // cumulative over each counter's alphas: N(alpha_k) = sum of bins <= k
@@ -1407,7 +1430,7 @@ lj_status lj_autotune(lj_system* s) {
       LJ_CUDA(s, cudaMemcpyAsync(s->records.p, snap_rec.p, sizeof(DevRecord) * s->records.n,
                                  cudaMemcpyDeviceToDevice, s->stream));
     // the fused steps' ticket counters follow the step parity restored here
-    LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * 4, s->stream));
+    LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n, s->stream));
     LJ_CUDA(s, cudaStreamSynchronize(s->stream));
     s->qpar = qpar;
     return LJ_OK;

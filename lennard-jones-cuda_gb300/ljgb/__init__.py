@@ -24,6 +24,7 @@ LIB_PATH = _build.LIB_PATH
 
 LJ_OK, LJ_ERR_INVALID, LJ_ERR_CUDA, LJ_ERR_NO_DEVICE = 0, 1, 2, 3
 LJ_ERR_DEVICE_TIMEOUT, LJ_ERR_NONFINITE, LJ_ERR_UNSUPPORTED, LJ_ERR_OUT_OF_MEMORY = 4, 5, 6, 7
+LJ_ERR_ESCAPED = 8
 BC_PERIODIC, BC_WALL, BC_NONE = 0, 1, 2
 PREC_MIXED, PREC_FP64 = 0, 1
 LATTICE_SC, LATTICE_FCC = 0, 1
@@ -124,6 +125,7 @@ def _declare(L):
         "threadExit": (None, []),
         "lj_counters_configure": (C.c_int, [_P, _P, C.c_int32, C.c_int32]),
         "lj_counters_read": (C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_int32)]),
+        "lj_counters_set_interval": (C.c_int, [_P, C.c_int32]),
         "lj_rdf_accumulate": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
         "lj_rdf_accumulated": (C.c_int, [_P, _P, C.POINTER(C.c_int64), C.c_int32]),
         "lj_render": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, _P]),
@@ -398,6 +400,10 @@ class System:
         arr = (Counter * max(1, len(counters)))(*[Counter(*c) for c in counters])
         self.counter_bins = sum(int(c[1]) for c in counters)
         self._c(load().lj_counters_configure(self.h, arr, len(counters), int(ring_steps)))
+
+    def counters_set_interval(self, every: int):
+        """Count after every `every`-th step only."""
+        self._c(load().lj_counters_set_interval(self.h, int(every)))
 
     def counters_read(self, max_steps: int = 1 << 20):
         n = C.c_int32()

@@ -103,7 +103,8 @@ def _build_into(lib_path: str, verbose: bool) -> str:
     return lib_path
 
 
-TASKS = {"ljgb-run-isotherm": "run_isotherm.cpp", "ljgb-run-fluctuations": "run_fluctuations.cpp"}
+TASKS = {"ljgb-run-isotherm": "run_isotherm.cpp", "ljgb-run-fluctuations": "run_fluctuations.cpp",
+         "ljgb-semiGCEfluctuations": "run_semigce_fluctuations.cpp"}
 TASK_DIR = os.path.join(PKG_DIR, "tasks")
 BIN_DIR = os.path.join(PKG_DIR, "bin")
 

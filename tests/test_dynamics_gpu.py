@@ -184,21 +184,32 @@ def test_launch_count_and_graph_reuse(ljgb_mod):
     w = ljgb_mod.System(n=1000, density=0.8, temperature=1.0, canonical=0, boundary=1)
     c3 = w.launch_count()
     w.integrate(0.005, 10)
-    # walls: drift, frame, quantize, pairs, reduce, observables per step
-    assert w.launch_count() - c3 == 6 * 10
+    assert w.launch_count() - c3 == 1 + 10     # walls keep a fixed frame: fused as well
+    o = ljgb_mod.System(n=1000, density=0.8, temperature=1.0, canonical=0, boundary=2)
+    c4 = o.launch_count()
+    o.integrate(0.005, 10)
+    # open box: drift, frame, quantize, pairs, reduce, observables per step
+    assert o.launch_count() - c4 == 6 * 10
 
 
-def test_fused_matches_unfused_path(ljgb_mod):
-    """The fused step (periodic) and the kernel-per-phase step (taken by
-    FP64 and non-periodic boxes) integrate the same equations: compare the
-    fused mixed path with the FP64 path over 30 steps of both ensembles."""
+@pytest.mark.parametrize("boundary", [0, 1])
+def test_fused_matches_unfused_path(ljgb_mod, boundary):
+    """The fused step (periodic and walled boxes) and the kernel-per-phase
+    step (taken by FP64 and open boxes) integrate the same equations: compare
+    the fused mixed path with the FP64 path over 30 steps of both ensembles.
+    With walls, one particle starts outside the box moving away from it: the
+    frame takes in the starting positions, and the wall turns it back."""
     import lj_testutil as U
     N, rho = 3000, 0.8
     pos, vel, L = U.lattice_state(N, rho, 1.1, "fcc", 0.02, seed=21)
+    if boundary == 1:
+        pos[7] = (L + 0.3, 0.5 * L, -0.2)
+        vel[7] = (2.0, 0.0, -1.0)
     for canonical in (0, 1):
         out = []
         for prec in (0, 1):
-            s = ljgb_mod.System(n=N, density=rho, temperature=1.0, canonical=canonical, precision=prec)
+            s = ljgb_mod.System(n=N, density=rho, temperature=1.0, canonical=canonical, precision=prec,
+                                boundary=boundary)
             s.set_state(pos, vel)
             s.calculate_forces()
             s.integrate(0.004, 15)
@@ -211,6 +222,8 @@ def test_fused_matches_unfused_path(ljgb_mod):
         for k in ("K", "V", "T", "P", "U", "t"):
             assert o0[k] == pytest.approx(o1[k], rel=1e-6, abs=1e-6), (canonical, k)
         assert o0["step"] == o1["step"] == 30 and o0["av_iters"] == o1["av_iters"] == 31
+        if boundary == 1:
+            assert p0[7, 0] < L + 0.3 + 0.1 and v0[7, 0] < 0    # turned back by the wall at x = L
 
 
 def test_autotune_keeps_the_state(ljgb_mod):

@@ -45,6 +45,11 @@ def test_statistics_match_reference_formulas(tmp_path, kind):
     assert got["n"] == n
     for k in ("mean", "var", "mean_err", "w", "w_err"):
         assert got[k] == pytest.approx(ref[k], rel=1e-9), k
+    # Statistics.hpp sums powers about the first observation: the reference
+    # with SetMeanShift(x[0])
+    cr = tasks.cumulant_ratios(x, shift=x[0])
+    for k in ("skew", "skew_err", "kurt", "kurt_err"):
+        assert got[k] == pytest.approx(cr[k], rel=1e-7), k
     s = tasks.inefficiency(x)
     assert got["s"] == pytest.approx(s, rel=1e-6)
     assert got["ta_err"] == pytest.approx(ref["mean_err"] * np.sqrt(s), rel=1e-6)
@@ -76,3 +81,18 @@ def test_task_executables_are_built(ljlib):
     import ljgb.build as b
     for name in b.TASKS:
         assert os.access(os.path.join(b.BIN_DIR, name), os.X_OK), name
+
+
+def test_gce_cube_count_is_the_type3_counter():
+    """GetNsub of the semi-grand-canonical task (cube of volume fraction f
+    around the centre) is the cumulative type-3 subsystem count at the same
+    accumulated fractions: the GPU counter serves both tasks."""
+    import tasks
+    fr = tasks.gce_fractions()
+    assert len(fr) == 19 and fr[-1] < 1.0 and fr[9] != 0.5   # accumulated, as the reference's loop
+    assert fr == tasks.alphas(0.05, False)
+    rng = np.random.default_rng(3)
+    L = 11.7
+    pos = rng.uniform(0, L, size=(3000, 3))
+    cum = tasks.subsystem_counts(pos, L, 0.05, 3)
+    assert [tasks.gce_nsub(pos, L, f) for f in fr] == list(cum)

@@ -1,7 +1,7 @@
 """Task-driver support on the GPU: the per-step subsystem counters and the
 RDF summed over steps, against the numpy restatement of the reference's
 counting functions (oracle/tasks.py) and the exact RDF emulation, on the
-positions and velocities of the same steps."""
+positions and velocities of the same steps; the task executables end to end."""
 import numpy as np
 import pytest
 
@@ -31,6 +31,28 @@ def test_subsystem_counters_match_reference_counting(ljgb_mod):
     assert s.counters_read().shape[0] == 0          # read clears
     # the cube of volume fraction 1 holds nothing beyond the box: last alpha < 1
     assert got[:, 3 * 19 + 18].max() <= N
+
+
+def test_counters_every_kth_step(ljgb_mod):
+    """lj_counters_set_interval: the central cubes counted after every 3rd
+    step only, against the restated GetNsub on the states of those steps."""
+    import tasks
+    N = 512
+    s = ljgb_mod.System(n=N, density=0.316, temperature=1.312)
+    s.counters_configure([(3, 19, 0.05, 0.0)], ring_steps=4)
+    s.counters_set_interval(3)
+    expect = []
+    for _ in range(4):
+        s.integrate(0.005, 3)
+        p, _, _ = s.get_state()
+        expect.append([tasks.gce_nsub(p, s.L, f) for f in tasks.gce_fractions()])
+    s.integrate(0.005, 2)                       # not a multiple of 3: no row
+    got = s.counters_read()
+    assert np.array_equal(got, np.array(expect))
+    s.integrate(0.005, 1)                       # the 15th step counts
+    assert s.counters_read().shape == (1, 19)
+    with pytest.raises(ljgb_mod.LJError):
+        s.counters_set_interval(0)
 
 
 def test_counter_ring_overflow_is_reported(ljgb_mod):
@@ -142,6 +164,36 @@ def test_run_fluctuations_driver(ljlib, tmp_path, ensemble):
     assert vz.shape == (20, 7)
     assert np.allclose(vz[:, 0], np.sqrt(1.4) * 3 * 0.05 * np.arange(1, 21), rtol=1e-5)  # 6 printed digits
     assert np.all(np.diff(vz[:, 1]) >= 0) and vz[-1, 2] > 0.95         # nearly all |v_z| < 3 sqrt(T*)
+
+
+def test_semigce_fluctuations_driver(ljlib, tmp_path):
+    """The semi-grand-canonical fluctuation task, shortened (500 TVN steps,
+    30 EVN events of 20 steps): the reference's console block every 10
+    events, and its statistics recomputed from the dumped per-event counts
+    with the restated NumberStatistics formulas."""
+    import tasks
+    r = _run_task("ljgb-semiGCEfluctuations", "N 512\nequilibration_steps 500\nsteps_per_event 20\nevents 30\n"
+                  "print_every 10\ndump_counts 1\noutput_prefix gce\n", tmp_path)
+    blocks = [b.splitlines() for b in r.stdout.strip().split("\n\n")]
+    assert len(blocks) == 3 and all(len(b) == 19 for b in blocks)
+    rows = [[float(x) for x in line.replace("+-", " ").split()] for line in blocks[-1]]
+    assert all(int(row[0]) == 30 for row in rows)
+    counts = np.loadtxt(tmp_path / "gce.counts.dat", ndmin=2)
+    assert counts.shape == (30, 19)
+    assert np.all(np.diff(counts, axis=1) >= 0) and counts.max() <= 512
+    fr = tasks.gce_fractions()
+    for k, (f, row) in enumerate(zip(fr, rows)):
+        x = counts[:, k]
+        m = tasks.moments(x)
+        want = [m["mean"], m["mean_err"], m["w"], m["w_err"], m["w"] / (1 - f), m["w_err"] / (1 - f)]
+        got = row[1:7]
+        if m["var"] > 0:
+            assert np.allclose(got, want, rtol=1e-5, atol=2e-6), (f, got, want)
+        assert abs(m["mean"] - f * 512) < 0.25 * f * 512 + 10           # <N> ~ f N
+        if m["var"] > 0 and abs(1 - 2 * f) > 1e-3:
+            cr = tasks.cumulant_ratios(x, shift=x[0])
+            assert row[7] == pytest.approx(cr["skew"] / (1 - 2 * f), rel=1e-5, abs=2e-6)
+            assert row[8] == pytest.approx(cr["skew_err"] / (1 - 2 * f), rel=1e-5, abs=2e-6)
 
 
 @pytest.mark.parametrize("axis,W,H", [(2, 96, 96), (0, 80, 64)])
