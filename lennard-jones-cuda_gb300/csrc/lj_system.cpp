@@ -49,6 +49,25 @@ struct DevBuf {
   }
 };
 
+// Page-locked host memory: the device writes into it with asynchronous
+// copies on the handle's stream, read by the host after one synchronisation.
+template <typename T>
+struct PinnedBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaHostAlloc(reinterpret_cast<void**>(&p), sizeof(T) * count, cudaHostAllocDefault);
+  }
+  void free() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
 struct GraphEntry {
   cudaGraph_t graph = nullptr;  // kept: exec-graph node updates name nodes of this graph
   cudaGraphExec_t exec = nullptr;
@@ -80,7 +99,11 @@ struct lj_system {
   int BI = 128;
 
   // device memory
-  DevBuf<double> x, v, f, tf, e, w, stage;
+  DevBuf<double> x, v, f, tf, e, w;
+  DevBuf<double> stage;          // 3 x (N,3) interleaved host-format arrays: positions, velocities, forces
+  DevBuf<int> bad;               // lowest index of a non-finite uploaded value (INT_MAX: none)
+  PinnedBuf<int> h_words;        // [0] status, [1] bad index: read back after one synchronisation
+  PinnedBuf<DevScalars> h_sc;    // per-box scalars read back
   DevBuf<int4> q, q2;  // fixed-point shadow, double-buffered for the fused step
   DevBuf<double4_32a> xd;
   DevBuf<int> blk_cnt, glob_cnt;  // fused-step completion counters
@@ -538,12 +561,12 @@ lj_status after_step(lj_system* s) {
   return LJ_OK;
 }
 
-lj_status check_status(lj_system* s) {
-  lj_status fst = flush_observables(s);
-  if (fst) return fst;
+// Waits for the handle's stream and reports the device status word, read
+// back by a copy enqueued behind the work (one synchronisation in all).
+lj_status sync_status(lj_system* s) {
+  LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
-  int st = 0;
-  LJ_CUDA(s, cudaMemcpy(&st, s->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+  const int st = s->h_words.p[0];
   if (st) {
     LJ_CUDA(s, cudaMemset(s->status.p, 0, sizeof(int)));
     // A failed launch may leave the fused-step counters mid-count.
@@ -562,6 +585,12 @@ lj_status check_status(lj_system* s) {
   return LJ_OK;
 }
 
+lj_status check_status(lj_system* s) {
+  lj_status fst = flush_observables(s);
+  if (fst) return fst;
+  return sync_status(s);
+}
+
 lj_status alloc_state(lj_system* s) {
   s->npad = (s->ntotal + 255) / 256 * 256;
   const size_t n3 = 3 * (size_t)s->npad;
@@ -569,7 +598,10 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, s->v.alloc(n3));
   LJ_CUDA(s, s->f.alloc(n3));
   LJ_CUDA(s, s->tf.alloc(n3));
-  LJ_CUDA(s, s->stage.alloc(n3));
+  LJ_CUDA(s, s->stage.alloc(3 * n3));
+  LJ_CUDA(s, s->bad.alloc(1));
+  LJ_CUDA(s, s->h_words.alloc(2));
+  LJ_CUDA(s, s->h_sc.alloc(s->nsys));
   LJ_CUDA(s, s->e.alloc(s->npad));
   LJ_CUDA(s, s->w.alloc(s->npad));
   LJ_CUDA(s, s->q.alloc(s->npad));
@@ -603,21 +635,21 @@ lj_status upload_xyz(lj_system* s, const double* host, double* dev) {
   return LJ_OK;
 }
 
-lj_status download_xyz(lj_system* s, const double* dev, double* host) {
-  const size_t bytes = sizeof(double) * 3 * (size_t)s->ntotal;
-  LJ_CUDA(s, launch_pack(dev, s->stage.p, s->ntotal, s->npad, s->stream));
-  s->launches += 1;
-  LJ_CUDA(s, cudaMemcpyAsync(host, s->stage.p, bytes, cudaMemcpyDeviceToHost, s->stream));
-  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
-  return LJ_OK;
+// Per-box scalars into the pinned mirror h_sc (check_status semantics: one
+// synchronisation, device status reported).
+lj_status fetch_scalars(lj_system* s) {
+  lj_status st = flush_observables(s);
+  if (st) return st;
+  LJ_CUDA(s, cudaMemcpyAsync(s->h_sc.p, s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
+  return sync_status(s);
 }
 
 lj_status read_scalars(lj_system* s, std::vector<DevScalars>& out) {
   lj_status st = flush_observables(s);
   if (st) return st;
-  out.resize(s->nsys);
-  LJ_CUDA(s, cudaMemcpyAsync(out.data(), s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(s->h_sc.p, s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  out.assign(s->h_sc.p, s->h_sc.p + s->nsys);
   return LJ_OK;
 }
 
@@ -786,6 +818,9 @@ lj_status lj_destroy(lj_system* s) {
   s->e.free();
   s->w.free();
   s->stage.free();
+  s->bad.free();
+  s->h_words.free();
+  s->h_sc.free();
   s->q.free();
   s->q2.free();
   s->xd.free();
@@ -838,34 +873,59 @@ lj_status lj_reinitialize(lj_system* s, const lj_config* cfg) {
   return LJ_OK;
 }
 
+// Both arrays go to the staging buffer in one pass and are checked there on
+// the device; the state is written only if every value is finite, so a
+// rejected call leaves it unchanged.  One synchronisation (the caller's
+// buffers are free on return).
 lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
   if (!s) return LJ_ERR_INVALID;
+  if (!pos && !vel) return LJ_OK;
   cudaSetDevice(s->device);
+  lj_status fst = flush_observables(s);
+  if (fst) return fst;
   s->pred_ready = false;
-  if (pos) {
-    for (size_t k = 0; k < 3 * (size_t)s->ntotal; ++k)
-      if (!std::isfinite(pos[k])) return fail(s, LJ_ERR_INVALID, "position %zu is not finite", k / 3);
-    lj_status st = upload_xyz(s, pos, s->x.p);
-    if (st) return st;
+  const size_t n3 = 3 * (size_t)s->ntotal;
+  double* st_pos = s->stage.p;
+  double* st_vel = s->stage.p + n3;
+  LJ_CUDA(s, cudaMemsetAsync(s->bad.p, 0x7f, sizeof(int), s->stream));
+  if (pos) LJ_CUDA(s, cudaMemcpyAsync(st_pos, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
+  if (vel) LJ_CUDA(s, cudaMemcpyAsync(st_vel, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, launch_check_finite(pos ? st_pos : st_vel, (pos && vel) ? 2 * n3 : n3, s->bad.p, s->stream));
+  if (pos) LJ_CUDA(s, launch_unpack_checked(st_pos, s->x.p, s->ntotal, s->npad, s->bad.p, s->stream));
+  if (vel) LJ_CUDA(s, launch_unpack_checked(st_vel, s->v.p, s->ntotal, s->npad, s->bad.p, s->stream));
+  s->launches += 1 + (pos ? 1 : 0) + (vel ? 1 : 0);
+  LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p + 1, s->bad.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  const int bad = s->h_words.p[1];
+  if (bad != 0x7f7f7f7f) {
+    const bool is_pos = pos && (size_t)bad < n3;
+    return fail(s, LJ_ERR_INVALID, "%s of particle %zu is not finite", is_pos ? "position" : "velocity",
+                ((size_t)bad % n3) / 3);
   }
-  if (vel) {
-    for (size_t k = 0; k < 3 * (size_t)s->ntotal; ++k)
-      if (!std::isfinite(vel[k])) return fail(s, LJ_ERR_INVALID, "velocity %zu is not finite", k / 3);
-    lj_status st = upload_xyz(s, vel, s->v.p);
-    if (st) return st;
-  }
+  // A walled box keeps its fixed-point frame between steps: rebuild it
+  // around the new positions.
+  if (pos && s->any_nonperiodic) return enqueue_frame_all(s);
   return LJ_OK;
 }
 
+// All requested arrays are packed and copied behind the pending work; one
+// synchronisation, which also reports the device status.
 lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
   if (!s) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);
-  lj_status st = check_status(s);
+  lj_status st = flush_observables(s);
   if (st) return st;
-  if (pos && (st = download_xyz(s, s->x.p, pos))) return st;
-  if (vel && (st = download_xyz(s, s->v.p, vel))) return st;
-  if (force && (st = download_xyz(s, s->f.p, force))) return st;
-  return LJ_OK;
+  const size_t n3 = 3 * (size_t)s->ntotal;
+  const double* src[3] = {s->x.p, s->v.p, s->f.p};
+  double* dst[3] = {pos, vel, force};
+  for (int k = 0; k < 3; ++k) {
+    if (!dst[k]) continue;
+    double* stg = s->stage.p + k * n3;
+    LJ_CUDA(s, launch_pack(src[k], stg, s->ntotal, s->npad, s->stream));
+    s->launches += 1;
+    LJ_CUDA(s, cudaMemcpyAsync(dst[k], stg, sizeof(double) * n3, cudaMemcpyDeviceToHost, s->stream));
+  }
+  return sync_status(s);
 }
 
 lj_status lj_get_pair_sums(lj_system* s, double* e, double* w) {
@@ -944,22 +1004,18 @@ lj_status lj_sync(lj_system* s) {
 lj_status lj_get_observables(lj_system* s, lj_observables* out) {
   if (!s || !out) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);
-  lj_status st = check_status(s);
+  lj_status st = fetch_scalars(s);
   if (st) return st;
-  std::vector<DevScalars> sc;
-  if ((st = read_scalars(s, sc))) return st;
-  fill_obs(sc[0], out);
+  fill_obs(s->h_sc.p[0], out);
   return LJ_OK;
 }
 
 lj_status lj_batch_observables(lj_system* s, lj_observables* out) {
   if (!s || !out) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);
-  lj_status st = check_status(s);
+  lj_status st = fetch_scalars(s);
   if (st) return st;
-  std::vector<DevScalars> sc;
-  if ((st = read_scalars(s, sc))) return st;
-  for (int k = 0; k < s->nsys; ++k) fill_obs(sc[k], out + k);
+  for (int k = 0; k < s->nsys; ++k) fill_obs(s->h_sc.p[k], out + k);
   return LJ_OK;
 }
 

@@ -243,3 +243,47 @@ def test_autotune_keeps_the_state(ljgb_mod):
     assert s.records() == r0
     s.integrate(0.005, 3)
     assert s.observables()["step"] == 8
+
+
+def test_set_state_checks_and_round_trips(ljgb_mod):
+    """lj_set_state checks finiteness on the device and leaves the state
+    unchanged when it rejects a call; set/get round-trip bit for bit."""
+    s = ljgb_mod.System(n=700, density=0.6, temperature=1.0, lattice=ljgb_mod.LATTICE_FCC, jitter=0.05)
+    s.integrate(0.005, 3)
+    p0, v0, f0 = s.get_state()
+    bad_v = v0.copy()
+    bad_v[5, 1] = np.nan
+    with pytest.raises(ljgb_mod.LJError, match="velocity of particle 5"):
+        s.set_state(p0 + 0.01, bad_v)
+    bad_p = p0.copy()
+    bad_p[3, 2] = np.inf
+    with pytest.raises(ljgb_mod.LJError, match="position of particle 3"):
+        s.set_state(bad_p, v0)
+    p1, v1, f1 = s.get_state()
+    assert np.array_equal(p1, p0) and np.array_equal(v1, v0) and np.array_equal(f1, f0)
+    rng = np.random.default_rng(1)
+    p2 = p0 + rng.normal(scale=1e-3, size=p0.shape)
+    v2 = v0 * 1.01
+    s.set_state(p2, None)
+    s.set_state(None, v2)
+    p3, v3, _ = s.get_state()
+    assert np.array_equal(p3, p2) and np.array_equal(v3, v2)
+    s.integrate(0.005, 2)
+    assert s.observables()["step"] == 5
+
+
+def test_walls_frame_follows_set_state(ljgb_mod):
+    """A walled box's fixed frame is rebuilt around positions set from the
+    host, even far outside the walls; the wall turns the particle back."""
+    N, rho = 864, 0.5
+    s = ljgb_mod.System(n=N, density=rho, temperature=1.0, boundary=1, lattice=ljgb_mod.LATTICE_FCC, jitter=0.02)
+    p, v, _ = s.get_state()
+    L = s.L
+    p[11] = (L + 4.0, 0.5 * L, 0.5 * L)      # 4 sigma beyond the wall, moving away
+    v[11] = (1.5, 0.0, 0.0)
+    s.set_state(p, v)
+    s.calculate_forces()
+    s.integrate(0.005, 400)
+    p1, v1, _ = s.get_state()
+    assert p1[11, 0] < L + 4.0 + 0.05 and v1[11, 0] < 0
+    assert np.all(p1 > -1.5) and np.all(p1 < L + 4.1)
