@@ -300,12 +300,18 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
             tb += pb;
           }
         } else {
-          // Ragged last tile of a box.
+          // Ragged last tile of a box: packed pairs with the self pair
+          // excluded, an odd last record on its own.
+          const int self = i_local - j0;
           for (int c0 = jlo; c0 < jhi; c0 += kChunk) {
-            float fx = 0.f, fy = 0.f, fz = 0.f, pa = 0.f, pb = 0.f;
             const int c1 = min(jhi, c0 + kChunk);
-            for (int jj = c0; jj < c1; ++jj)
-              pair_mixed<true>(qi, st[jj], k2inv, j0 + jj == i_local, fx, fy, fz, pa, pb);
+            const f32x2 k2i2 = pk2(k2inv, k2inv);
+            f32x2 FX = 0ull, FY = 0ull, FZ = 0ull, PA = 0ull, PB = 0ull;
+            int jj = c0;
+            for (; jj + 1 < c1; jj += 2)
+              pair_mixed2<true>(qi, st[jj], st[jj + 1], k2i2, jj == self, jj + 1 == self, FX, FY, FZ, PA, PB);
+            float fx = lane_sum(FX), fy = lane_sum(FY), fz = lane_sum(FZ), pa = lane_sum(PA), pb = lane_sum(PB);
+            if (jj < c1) pair_mixed<true>(qi, st[jj], k2inv, jj == self, fx, fy, fz, pa, pb);
             two_sum_add(acc[0], fx);
             two_sum_add(acc[1], fy);
             two_sum_add(acc[2], fz);
