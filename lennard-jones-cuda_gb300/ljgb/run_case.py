@@ -32,7 +32,22 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--shape", type=int, default=-1, help="pair-kernel shape (-1: autotune)")
     ap.add_argument("--time-shapes", action="store_true", help="print the pair-kernel time of every shape")
+    ap.add_argument("--adjoint", type=int, default=0, metavar="K",
+                    help="run the adjoint instead (EVN, FP64, checkpoints every K steps): forward + backward "
+                         "of loss = <V/N + P> over --steps steps")
     a = ap.parse_args(argv)
+    if a.adjoint > 0:
+        adj = ljgb.Adjoint(n=a.n, density=a.rho, temperature=a.T, lattice=ljgb.LATTICE_FCC if a.fcc else
+                           ljgb.LATTICE_SC, jitter=a.jitter, seed=a.seed, checkpoint_every=a.adjoint)
+        adj.set_loss(0.0, 1.0, 1.0)
+        t0 = time.perf_counter()
+        loss = adj.forward(a.dt, a.steps)
+        t1 = time.perf_counter()
+        de, ds, dx, _ = adj.backward()
+        t2 = time.perf_counter()
+        print("adjoint n=%d steps=%d loss=%.10f dloss/deps=%.6e dloss/dsigma=%.6e |dloss/dx0|max=%.3e "
+              "forward=%.3fs backward=%.3fs" % (a.n, a.steps, loss, de, ds, abs(dx).max(), t1 - t0, t2 - t1))
+        return
     s = ljgb.System(n=a.n, density=a.rho, temperature=a.T, canonical=int(a.tvn), boundary=a.bc,
                     lattice=ljgb.LATTICE_FCC if a.fcc else ljgb.LATTICE_SC, jitter=a.jitter, seed=a.seed,
                     precision=ljgb.PREC_FP64 if a.fp64 else ljgb.PREC_MIXED)
