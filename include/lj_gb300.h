@@ -218,6 +218,14 @@ lj_status lj_profile_read(lj_system* sys, int64_t* pair_launches, double* pair_m
 lj_status lj_get_stream(lj_system* sys, void** stream);
 lj_status lj_set_stream(lj_system* sys, void* stream);
 
+/* Self-test of the device-side wait limit (no counterpart in the reference,
+ * whose kernels have no waits).  Runs the bounded mbarrier wait of the pair
+ * kernels on a barrier that nothing completes: it must give up after its
+ * 1.5 s limit, flag LJ_DEVFLAG_TIMEOUT and return, and the host must report
+ * LJ_ERR_DEVICE_TIMEOUT.  Returns LJ_OK when that happened (the handle stays
+ * usable), LJ_ERR_CUDA otherwise.  Takes about 1.5 s. */
+lj_status lj_selftest_device_timeout(lj_system* sys);
+
 /* Number of kernels the library launched on this handle since creation. */
 int64_t lj_kernel_launch_count(const lj_system* sys);
 

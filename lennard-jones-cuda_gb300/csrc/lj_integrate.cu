@@ -544,9 +544,29 @@ __global__ void k_unpack_checked(const double* __restrict__ in, double* __restri
   for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
 }
 
+// A wait that nothing completes: the pair kernels' bounded mbarrier wait must
+// give up after its limit, flag LJ_DEVFLAG_TIMEOUT and let the kernel return.
+__global__ void k_selftest_wait(int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (!mbar_wait_bounded(&bar, 0)) atomicOr(status, LJ_DEVFLAG_TIMEOUT);
+    mbar_inval(&bar);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Launchers.
 // ---------------------------------------------------------------------------
+cudaError_t launch_selftest_wait(int* status, cudaStream_t st) {
+  k_selftest_wait<<<1, 32, 0, st>>>(status);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_check_finite(const double* in, size_t count, int* bad, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   k_check_finite<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, (long long)count, bad);

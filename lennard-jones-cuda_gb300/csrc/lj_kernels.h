@@ -134,6 +134,7 @@ cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, in
                             cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st);
+cudaError_t launch_selftest_wait(int* status, cudaStream_t st);
 cudaError_t launch_check_finite(const double* in, size_t count, int* bad, cudaStream_t st);
 cudaError_t launch_unpack_checked(const double* in, double* out, int n, int npad, const int* bad, cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,

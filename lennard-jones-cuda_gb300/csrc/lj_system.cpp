@@ -1531,6 +1531,19 @@ lj_status lj_autotune(lj_system* s) {
   return LJ_OK;
 }
 
+lj_status lj_selftest_device_timeout(lj_system* s) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = check_status(s);  // earlier errors are reported as such
+  if (st) return st;
+  LJ_CUDA(s, launch_selftest_wait(s->status.p, s->stream));
+  s->launches += 1;
+  st = sync_status(s);
+  if (st == LJ_ERR_DEVICE_TIMEOUT) return LJ_OK;
+  if (st) return st;
+  return fail(s, LJ_ERR_CUDA, "the bounded device wait returned without reporting its timeout");
+}
+
 lj_status lj_profile_enable(lj_system* s, int32_t on) {
   if (!s) return LJ_ERR_INVALID;
   cudaSetDevice(s->device);

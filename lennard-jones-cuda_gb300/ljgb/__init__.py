@@ -126,6 +126,7 @@ def _declare(L):
         "lj_counters_configure": (C.c_int, [_P, _P, C.c_int32, C.c_int32]),
         "lj_counters_read": (C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_int32)]),
         "lj_counters_set_interval": (C.c_int, [_P, C.c_int32]),
+        "lj_selftest_device_timeout": (C.c_int, [_P]),
         "lj_rdf_accumulate": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
         "lj_rdf_accumulated": (C.c_int, [_P, _P, C.POINTER(C.c_int64), C.c_int32]),
         "lj_render": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, _P]),
@@ -400,6 +401,11 @@ class System:
         arr = (Counter * max(1, len(counters)))(*[Counter(*c) for c in counters])
         self.counter_bins = sum(int(c[1]) for c in counters)
         self._c(load().lj_counters_configure(self.h, arr, len(counters), int(ring_steps)))
+
+    def selftest_device_timeout(self):
+        """Runs a device wait that nothing completes; raises unless its
+        timeout was reported (the handle stays usable)."""
+        self._c(load().lj_selftest_device_timeout(self.h))
 
     def counters_set_interval(self, every: int):
         """Count after every `every`-th step only."""

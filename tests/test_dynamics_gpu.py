@@ -287,3 +287,20 @@ def test_walls_frame_follows_set_state(ljgb_mod):
     p1, v1, _ = s.get_state()
     assert p1[11, 0] < L + 4.0 + 0.05 and v1[11, 0] < 0
     assert np.all(p1 > -1.5) and np.all(p1 < L + 4.1)
+
+
+def test_device_wait_limit_reports_and_recovers(ljgb_mod):
+    """The pair kernels' bounded mbarrier wait, on a barrier nothing
+    completes: it gives up after its 1.5 s limit, the host reports
+    LJ_ERR_DEVICE_TIMEOUT (the self-test returns normally), and the same
+    handle steps on.  No fault and no hang are involved."""
+    import time
+    s = ljgb_mod.System(n=500, density=0.8, temperature=1.0, canonical=1)
+    s.integrate(0.005, 2)
+    t0 = time.perf_counter()
+    s.selftest_device_timeout()
+    el = time.perf_counter() - t0
+    assert 1.4 < el < 30
+    s.integrate(0.005, 3)
+    o = s.observables()
+    assert o["step"] == 5 and np.isfinite(o["U"])
