@@ -366,28 +366,37 @@ __global__ void k_predict(StateArgs s) {
 __global__ void k_tvn_close(StateArgs s) {
   __shared__ double sh[3 * 32];
   // Launched as a programmatic dependent of the pair kernel: the CTAs start
-  // while the pair grid drains and wait here until its writes are visible.
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  // while the pair grid drains.  What the pair kernel does not write (the
+  // block table, the box, x, v and F_n) is loaded before waiting for its
+  // writes (F_{n+1} in tf, e, w, chi) to become visible.
   const int B = blockIdx.x;
   const BlockInfo bi = s.blocks[B];
   const int tid = threadIdx.x;
   const BoxArgs box = s.boxes[bi.sys];
+  const bool valid = tid < bi.n_i;
+  const int p = bi.p0 + bi.i0 + (valid ? tid : 0);
+  double xn[3], vn[3], fn[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = (size_t)c * s.npad + p;
+    xn[c] = s.x[k];
+    vn[c] = s.v[k];
+    fn[c] = s.f[k];
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   DevScalars& sc = s.sc[bi.sys];
   const double chi = sc.chi;
   const double a1 = 2. * chi - 1., b1 = chi * box.dt;
   double part[3] = {0.0, 0.0, 0.0};
-  if (tid < bi.n_i) {
-    const int p = bi.p0 + bi.i0 + tid;
+  if (valid) {
     double x[3], v[3], f1[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t k = (size_t)c * s.npad + p;
-      const double fn = s.f[k];
       f1[c] = s.tf[k];
-      const double tf = 0.5 * fn + 0.5 * f1[c];
-      const double v0 = s.v[k];
-      x[c] = drift_pos(box, s.x[k], v0, fn);
-      v[c] = fma(a1, v0, b1 * tf);
+      const double tf = 0.5 * fn[c] + 0.5 * f1[c];
+      x[c] = drift_pos(box, xn[c], vn[c], fn[c]);
+      v[c] = fma(a1, vn[c], b1 * tf);
     }
     apply_bc(box.bc, box.L, x, v);
     double xp[3];

@@ -107,6 +107,27 @@ def test_energy_conservation_and_momentum(ljgb_mod):
     assert abs(drift[0] - drift[1]) < 1e-4
 
 
+def test_wall_energy_conservation_fused_vs_fp64(ljgb_mod):
+    """EVN between hard walls (N=500, rho*=0.3, T*=1.4, 2000 steps): a wall
+    flips a velocity component and keeps K, so U is conserved as in a
+    periodic box.  The fused mixed path (fixed wall frame) and the FP64
+    kernel-per-phase path conserve it alike."""
+    N, rho = 500, 0.3
+    drift = {}
+    for prec in (0, 1):
+        s = ljgb_mod.System(n=N, density=rho, temperature=1.4, boundary=1, lattice=ljgb_mod.LATTICE_FCC,
+                            jitter=0.05, seed=11, precision=prec)
+        U0 = s.observables()["U"]
+        s.set_recording(2000)
+        s.integrate(0.002, 2000)
+        Us = np.array([r["U"] for r in s.records()])
+        p, _, _ = s.get_state()
+        assert p.min() > -0.5 and p.max() < s.L + 0.5
+        drift[prec] = np.abs(Us - U0).max() / N
+    assert drift[0] < 2e-3 and drift[1] < 2e-3
+    assert abs(drift[0] - drift[1]) < 2e-4
+
+
 def test_wall_keeps_particles_in_box(ljgb_mod):
     N, rho = 500, 0.3
     s = ljgb_mod.System(n=N, density=rho, temperature=2.0, boundary=1, jitter=0.05, seed=7)
