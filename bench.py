@@ -349,6 +349,54 @@ def replica_value(world: int, pairs_per_step: int, steps: int, total_ms: float) 
     return world * pairs_per_step * steps / (total_ms * 1e-3)
 
 
+def ref_gpu_kernel(torch, ljgb, dev, flush, pair_ms, steps=20, block=256):
+    """The reference's GPU force kernel, restated in comparator/ref_nbody.cu
+    (FP32 nbody tiles, lround minimum image, a global RDF atomic per pair),
+    timed on the bench state: informational, beside the library's pair
+    kernel."""
+    import ctypes as C
+    import ljgb.build as B
+    lib = C.CDLL(B.COMPARATOR_LIB)
+    lib.ljref_scratch_bytes.restype = C.c_size_t
+    lib.ljref_scratch_bytes.argtypes = [C.c_int, C.c_int]
+    lib.ljref_forces.restype = C.c_int
+    lib.ljref_forces.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_float, C.c_int,
+                                 C.c_void_p, C.c_void_p]
+    s = make_system(ljgb, 0, dev)
+    pos, _, _ = s.get_state()
+    L = s.L
+    s.close()
+    p4 = torch.zeros((N, 4), dtype=torch.float32, device="cuda")
+    p4[:, :3] = torch.from_numpy(pos.astype(np.float32)).cuda()
+    f4 = torch.zeros_like(p4)
+    scratch = torch.zeros(int(lib.ljref_scratch_bytes(N, block)) // 4 + 4, dtype=torch.int32, device="cuda")
+    dr2 = float(ljgb.reference_rdf_dr2(N))
+    stream = torch.cuda.current_stream()
+
+    def run():
+        rc = lib.ljref_forces(p4.data_ptr(), f4.data_ptr(), N, L, 1, dr2, block, scratch.data_ptr(),
+                              stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError("ljref_forces failed: cuda error %d" % rc)
+
+    for _ in range(3):
+        run()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record()
+        run()
+        b.record()
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    return {"kind": "restatement of the reference's calculateForces kernel (MDSystem.cu:21-153, "
+                    "comparator/ref_nbody.cu), block %d, RDF counted per pair" % block,
+            "ms_per_eval": ms, "pair_interactions_per_s": N * (N - 1) / (ms * 1e-3),
+            "library_pair_kernel_speedup": ms / pair_ms,
+            "note": "force evaluation only (the reference's host-side Verlet step and per-call allocations "
+                    "are not timed); L2 flushed before every launch"}
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import ljgb
@@ -408,6 +456,7 @@ def gpu_arm(args, rank, world, local_rank):
         traffic = read_traffic()
         cpu = cpu_baseline(max_seconds=args.cpu_seconds)
         extra = extra_configs(torch, ljgb, oracle, dev, flush, peak) if not args.no_extra else None
+        refk = ref_gpu_kernel(torch, ljgb, dev, flush, pair_ms)
         result = {
             "metric": "pair-interactions/s, N=16384, FP32-mixed vs FP64 same GB300 @ force rel err<=1e-5",
             "value": value, "unit": "pair-interactions/s", "n_gpus": world, "steps": args.steps,
@@ -431,6 +480,7 @@ def gpu_arm(args, rank, world, local_rank):
                          "peak_source": "nominal FP32: %d SMs x 128 lanes x 2 x %.0f MHz (MEASURED_PEAKS.json "
                                         "has no FP32 figure)" % (sms, mhz)},
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "ref_gpu_kernel": refk,
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }
