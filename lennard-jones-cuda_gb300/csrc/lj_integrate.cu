@@ -483,6 +483,7 @@ __global__ void k_velocity_hist(StateArgs s, double step, int nb, unsigned long 
   for (int b = threadIdx.x; b < nb; b += blockDim.x) hist[b] = 0u;
   __syncthreads();
   const BlockInfo bi = s.blocks[blockIdx.x];
+  int bin = -1;
   if ((int)threadIdx.x < bi.n_i) {
     const int p = bi.p0 + bi.i0 + threadIdx.x;
     const double vx = s.v[p], vy = s.v[(size_t)s.npad + p], vz = s.v[2 * (size_t)s.npad + p];
@@ -490,8 +491,12 @@ __global__ void k_velocity_hist(StateArgs s, double step, int nb, unsigned long 
     q = __dadd_rn(q, __dmul_rn(vy, vy));
     q = __dadd_rn(q, __dmul_rn(vz, vz));
     const double b = floor(__ddiv_rn(__dsqrt_rn(q), step));
-    if (b < (double)nb) atomicAdd(&hist[(int)b], 1u);
+    if (b < (double)nb) bin = (int)b;
   }
+  // warp-aggregated: the lanes with the same bin add once (speeds cluster
+  // in a few bins around sqrt(2 T))
+  const unsigned peers = __match_any_sync(0xffffffffu, bin);
+  if (bin >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     if (hist[b]) atomicAdd(counts + b, (unsigned long long)hist[b]);
