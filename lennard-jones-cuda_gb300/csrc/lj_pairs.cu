@@ -145,21 +145,30 @@ __device__ __forceinline__ float lane_sum(f32x2 v) {
   return a + b;
 }
 
+// floor(x) for 0 <= x < 2^23: 2^23 + x rounded down is 2^23 + floor(x)
+// exactly, read back from the float's bits (an FP32 add and an integer
+// subtract instead of a round and a float -> int conversion).
+__device__ __forceinline__ int floor_small(float x) {
+  return __float_as_int(__fadd_rd(x, 8388608.0f)) - 0x4B000000;
+}
+
 // Histogram bin of a pair from its fixed-point separation; the arithmetic is
-// exactly what the oracle's emu_rdf_* reproduces on the CPU.
+// exactly what the oracle's emu_rdf_* reproduces on the CPU (floor of the
+// separately rounded products, clamped or dropped past the last bin).
 __device__ __forceinline__ int pair_bin(const int4 qi, const int4 qj, float k2, const HistArgs& h) {
   const float dx = __int2float_rn((int)((unsigned)qj.x - (unsigned)qi.x));
   const float dy = __int2float_rn((int)((unsigned)qj.y - (unsigned)qi.y));
   const float dz = __int2float_rn((int)((unsigned)qj.z - (unsigned)qi.z));
   const float r2 = __fmul_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), k2);
-  if (h.mode == 2) {  // linear r bins, r < rmax
+  if (h.mode == 2) {  // linear r bins, r < rmax (so r / w < nb, up to rounding)
     if (!(r2 < h.rmax2)) return -1;
-    int b = (int)floorf(__fmul_rn(__fsqrt_rn(r2), h.inv_w));
-    return b > h.nb - 1 ? h.nb - 1 : b;
+    return min(floor_small(__fmul_rn(__fsqrt_rn(r2), h.inv_w)), h.nb - 1);
   }
-  const float fb = floorf(__fmul_rn(r2, h.inv_w));
-  if (h.mode == 0) return fb < (float)(h.nb - 1) ? (int)fb : h.nb - 1;  // clamp (MDSystem.cu:39)
-  return fb < (float)h.nb ? (int)fb : -1;                               // drop (MDSystem.cpp:283)
+  // r^2 bins; the quotient is capped at nb first, which keeps it in
+  // floor_small's range and changes no bin
+  const int fb = floor_small(fminf(__fmul_rn(r2, h.inv_w), (float)h.nb));
+  if (h.mode == 0) return min(fb, h.nb - 1);  // clamp (MDSystem.cu:39)
+  return fb < h.nb ? fb : -1;                  // drop (MDSystem.cpp:283)
 }
 
 }  // namespace
