@@ -260,9 +260,10 @@ lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_
                            int32_t* out_ctas, int32_t* out_nseg, int32_t* cta_tile_begin, int32_t* cta_lo,
                            int32_t* block_info, int32_t max_blocks);
 
-/* All-pairs LJ forces for callers that cannot allocate device memory (code
- * running inside another framework's memory pool or a stream capture, loops
- * that must not allocate after start-up, embedders whose allocator owns the
+/* All-pairs LJ forces for callers that cannot allocate device memory
+ * (plug-ins inside a framework whose caching allocator has reserved the GPU's
+ * memory, loops that must not allocate after start-up because cudaMalloc and
+ * cudaFree can synchronise the device, embedders whose allocator owns the
  * GPU).  No counterpart in the reference.  pos4: device float4[n] positions
  * (w ignored); force4: device float4[n] out, xyz = force (eps = sigma = 1),
  * w = sum_j (r^-12 - r^-6), as calculateNForces writes Force; sums (host,

@@ -1,10 +1,11 @@
 // lj_noalloc.cu -- all-pairs LJ forces without any device allocation.
 //
-// Some callers cannot allocate device memory: code that runs inside another
-// framework's memory pool or a captured stream (where cudaMalloc is
-// forbidden or would serialise the device), real-time loops that must not
-// allocate after start-up, and embedders whose allocator owns every byte of
-// the GPU.  lj_forces_static serves them: the caller passes device input and
+// Some callers cannot allocate device memory: plug-ins hosted by another
+// framework whose caching allocator has reserved the GPU's memory (a
+// cudaMalloc of their own fails or fragments that pool), real-time loops
+// that must not allocate after start-up (cudaMalloc and cudaFree can
+// synchronise the whole device and stall every stream), and embedders whose
+// rules give every byte of the GPU to their own allocator.  lj_forces_static serves them: the caller passes device input and
 // output arrays only, and every intermediate buffer (fixed-point shadow, work
 // schedule, per-segment partial sums, block sums, status word) lives in one
 // file-scope __device__ array of fixed size that each GPU holds from the
