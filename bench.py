@@ -61,32 +61,44 @@ WORKLOAD = "lj-dense-liquid-tvn N=16384 rho*=0.85 T*=1.0 FCC+0.02 dt=0.005"
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples taken while the timed
+    region runs.  The sampler is started and its first line awaited before
+    the region begins (nvidia-smi needs ~0.1-0.5 s to come up); only samples
+    stamped inside the region (plus one interval after it) are summarised."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 20
 
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (monotonic time, line)
+        self.t_begin = self.t_end = None
+        self._first = threading.Event()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.INTERVAL_MS)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self._first.wait(timeout=5.0)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self.t_begin = time.monotonic()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+            self._first.set()
 
     def __exit__(self, *exc):
+        self.t_end = time.monotonic()
         if self.proc:
+            time.sleep(self.INTERVAL_MS * 1e-3)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -96,7 +108,10 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        t_hi = (self.t_end or time.monotonic()) + self.INTERVAL_MS * 1e-3
+        for t, ln in self.lines:
+            if self.t_begin is not None and not (self.t_begin <= t <= t_hi):
+                continue
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -109,7 +124,8 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "interval_ms": self.INTERVAL_MS,
+                "region_s": (self.t_end - self.t_begin) if self.t_end and self.t_begin else None}
 
 
 # ---------------------------------------------------------------------------
@@ -188,23 +204,22 @@ def timed_steps(torch, s, steps, warmup, flush, dt=DT):
 
 def e2e_steps(ljgb, s, steps, warmup):
     """Through the public API with host buffers: per step upload pos+vel from
-    pinned memory, one step, download pos+vel and the observables."""
+    pinned memory (lj_set_state), one step (lj_step), download pos+vel and the
+    observables (lj_get_state_observables)."""
     pos = ljgb.pinned((N, 3))
     vel = ljgb.pinned((N, 3))
     s.get_state_into(pos, vel, None)
     for _ in range(warmup):
         s.set_state_from(pos, vel)
         s.integrate(DT)
-        s.get_state_into(pos, vel, None)
-        s.observables()
+        s.get_state_observables_into(pos, vel, None)
     t0 = time.perf_counter()
     for _ in range(steps):
         s.set_state_from(pos, vel)
         s.integrate(DT)
-        s.get_state_into(pos, vel, None)
-        s.observables()
+        s.get_state_observables_into(pos, vel, None)
     el = time.perf_counter() - t0
-    obs_bytes = 14 * 8
+    obs_bytes = 208 + 4  # the box's device scalar block (observables, clock, averages) and the status word
     return el, {"h2d_bytes_per_step": 2 * N * 3 * 8, "d2h_bytes_per_step": 2 * N * 3 * 8 + obs_bytes}
 
 
@@ -531,7 +546,7 @@ def reference_arm(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

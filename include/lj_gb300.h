@@ -158,6 +158,13 @@ lj_status lj_sync(lj_system* sys);
 /* Observables after the last step / force evaluation (synchronises). */
 lj_status lj_get_observables(lj_system* sys, lj_observables* out);
 
+/* lj_get_state and lj_get_observables in one call with one synchronisation:
+ * what a host loop that mirrors the state every step (the reference's
+ * Integrate followed by getArray, MDSystem.cpp:438-583, 586-613) needs.  Any
+ * pointer may be NULL. */
+lj_status lj_get_state_observables(lj_system* sys, double* pos, double* vel, double* force,
+                                   lj_observables* out);
+
 /* Per-step observable records.  lj_set_recording(sys, cap) keeps the last
  * cap steps (0 disables); lj_get_records copies up to max records, oldest
  * first, and returns their count in *count. */

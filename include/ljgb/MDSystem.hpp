@@ -158,5 +158,6 @@ class MDSystem {
   void pullObservables(bool parameters);
   void pullRDF();
   void mirrorFromDevice();
+  void fillMirrors();
   void pushArrays(bool pos, bool vel);
 };

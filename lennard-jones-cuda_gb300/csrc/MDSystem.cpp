@@ -277,7 +277,18 @@ void MDSystem::Integrate(double dt, int nsteps) {
   lj_observables o0, o1;
   if (!check(lj_get_observables(m_sys, &o0))) return;
   if (!check(lj_step(m_sys, dt, nsteps))) return;
-  if (!check(lj_get_observables(m_sys, &o1))) return;
+  // With host mirrors on, the state and the observables come back together.
+  const bool mirrored = m_mirror && h_Pos;
+  if (mirrored) {
+    const int N = m_config.N;
+    m_buf.resize(3 * (size_t)N);
+    m_buf2.resize(3 * (size_t)N);
+    m_buf3.resize(3 * (size_t)N);
+    if (!check(lj_get_state_observables(m_sys, m_buf.data(), m_buf2.data(), m_buf3.data(), &o1))) return;
+    fillMirrors();
+  } else if (!check(lj_get_observables(m_sys, &o1))) {
+    return;
+  }
   K = o1.K;
   V = o1.V;
   T = o1.T;
@@ -290,7 +301,6 @@ void MDSystem::Integrate(double dt, int nsteps) {
   av_p_tot += o1.av_p_tot - o0.av_p_tot;
   av_T_tot += o1.av_T_tot - o0.av_T_tot;
   if (m_rdf_every_step) pullRDF();
-  if (m_mirror) mirrorFromDevice();
 }
 
 // MDSystem::getArray (MDSystem.cpp:586-613)
@@ -446,6 +456,12 @@ void MDSystem::mirrorFromDevice() {
   m_buf2.resize(3 * (size_t)N);
   m_buf3.resize(3 * (size_t)N);
   if (!check(lj_get_state(m_sys, m_buf.data(), m_buf2.data(), m_buf3.data()))) return;
+  fillMirrors();
+}
+
+// h_Pos / h_Vel / h_Force from the FP64 buffers last read from the device.
+void MDSystem::fillMirrors() {
+  const int N = m_config.N;
   const float w = (float)(L / 150.f);
   for (int i = 0; i < N; ++i) {
     for (int c = 0; c < 3; ++c) {

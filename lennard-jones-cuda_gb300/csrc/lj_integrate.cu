@@ -541,21 +541,34 @@ __global__ void k_pack(const double* __restrict__ in, double* __restrict__ out, 
   for (int c = 0; c < 3; ++c) out[3 * (size_t)i + c] = in[(size_t)c * npad + i];
 }
 
+// Up to three (N,3) <-> component-major transposes in one launch; blockIdx.y
+// selects the array.
+__global__ void k_pack_multi(XyzArrays a, int n, int npad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* __restrict__ in = a.src[blockIdx.y];
+  double* __restrict__ out = a.dst[blockIdx.y];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[3 * (size_t)i + c] = in[(size_t)c * npad + i];
+}
+
+// k_unpack for up to three arrays, skipped when k_check_finite found a
+// non-finite value.
+__global__ void k_unpack_multi_checked(XyzArrays a, int n, int npad, const int* bad) {
+  if (*bad != 0x7f7f7f7f) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* __restrict__ in = a.src[blockIdx.y];
+  double* __restrict__ out = a.dst[blockIdx.y];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
+}
+
 // Lowest index of a non-finite value among `count` staged values (bad starts
 // at 0x7f7f7f7f).
 __global__ void k_check_finite(const double* __restrict__ in, long long count, int* bad) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count && !isfinite(in[i])) atomicMin(bad, (int)i);
-}
-
-// k_unpack, skipped when k_check_finite found a non-finite value.
-__global__ void k_unpack_checked(const double* __restrict__ in, double* __restrict__ out, int n, int npad,
-                                 const int* bad) {
-  if (*bad != 0x7f7f7f7f) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
 }
 
 // A wait that nothing completes: the pair kernels' bounded mbarrier wait must
@@ -587,13 +600,21 @@ cudaError_t launch_check_finite(const double* in, size_t count, int* bad, cudaSt
   return cudaGetLastError();
 }
 
-cudaError_t launch_unpack_checked(const double* in, double* out, int n, int npad, const int* bad, cudaStream_t st) {
-  k_unpack_checked<<<(n + 255) / 256, 256, 0, st>>>(in, out, n, npad, bad);
+cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st) {
+  k_unpack<<<(n + 255) / 256, 256, 0, st>>>(in, out, n, npad);
   return cudaGetLastError();
 }
 
-cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st) {
-  k_unpack<<<(n + 255) / 256, 256, 0, st>>>(in, out, n, npad);
+cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_pack_multi<<<dim3((n + 255) / 256, count), 256, 0, st>>>(a, n, npad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_multi_checked(const XyzArrays& a, int count, int n, int npad, const int* bad,
+                                        cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_unpack_multi_checked<<<dim3((n + 255) / 256, count), 256, 0, st>>>(a, n, npad, bad);
   return cudaGetLastError();
 }
 

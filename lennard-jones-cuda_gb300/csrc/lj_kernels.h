@@ -136,7 +136,14 @@ cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaSt
 cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_selftest_wait(int* status, cudaStream_t st);
 cudaError_t launch_check_finite(const double* in, size_t count, int* bad, cudaStream_t st);
-cudaError_t launch_unpack_checked(const double* in, double* out, int n, int npad, const int* bad, cudaStream_t st);
+// Up to three (N,3) interleaved <-> component-major [3][npad] transposes in one launch.
+struct XyzArrays {
+  const double* src[3];
+  double* dst[3];
+};
+cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, cudaStream_t st);
+cudaError_t launch_unpack_multi_checked(const XyzArrays& a, int count, int n, int npad, const int* bad,
+                                        cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,
                                     cudaStream_t st);
 

@@ -891,9 +891,18 @@ lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
   if (pos) LJ_CUDA(s, cudaMemcpyAsync(st_pos, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
   if (vel) LJ_CUDA(s, cudaMemcpyAsync(st_vel, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
   LJ_CUDA(s, launch_check_finite(pos ? st_pos : st_vel, (pos && vel) ? 2 * n3 : n3, s->bad.p, s->stream));
-  if (pos) LJ_CUDA(s, launch_unpack_checked(st_pos, s->x.p, s->ntotal, s->npad, s->bad.p, s->stream));
-  if (vel) LJ_CUDA(s, launch_unpack_checked(st_vel, s->v.p, s->ntotal, s->npad, s->bad.p, s->stream));
-  s->launches += 1 + (pos ? 1 : 0) + (vel ? 1 : 0);
+  XyzArrays xa{};
+  int na = 0;
+  if (pos) {
+    xa.src[na] = st_pos;
+    xa.dst[na++] = s->x.p;
+  }
+  if (vel) {
+    xa.src[na] = st_vel;
+    xa.dst[na++] = s->v.p;
+  }
+  LJ_CUDA(s, launch_unpack_multi_checked(xa, na, s->ntotal, s->npad, s->bad.p, s->stream));
+  s->launches += 2;
   LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p + 1, s->bad.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   const int bad = s->h_words.p[1];
@@ -908,6 +917,29 @@ lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
   return LJ_OK;
 }
 
+// Packs the requested arrays (one launch) and queues their copies to the
+// host behind the pending work; the caller synchronises.
+static lj_status enqueue_state_read(lj_system* s, double* pos, double* vel, double* force) {
+  const size_t n3 = 3 * (size_t)s->ntotal;
+  const double* src[3] = {s->x.p, s->v.p, s->f.p};
+  double* dst[3] = {pos, vel, force};
+  XyzArrays xa{};
+  double* host[3] = {nullptr, nullptr, nullptr};
+  int na = 0;
+  for (int k = 0; k < 3; ++k) {
+    if (!dst[k]) continue;
+    xa.src[na] = src[k];
+    xa.dst[na] = s->stage.p + na * n3;
+    host[na++] = dst[k];
+  }
+  if (na == 0) return LJ_OK;
+  LJ_CUDA(s, launch_pack_multi(xa, na, s->ntotal, s->npad, s->stream));
+  s->launches += 1;
+  for (int k = 0; k < na; ++k)
+    LJ_CUDA(s, cudaMemcpyAsync(host[k], xa.dst[k], sizeof(double) * n3, cudaMemcpyDeviceToHost, s->stream));
+  return LJ_OK;
+}
+
 // All requested arrays are packed and copied behind the pending work; one
 // synchronisation, which also reports the device status.
 lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
@@ -915,17 +947,25 @@ lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
   cudaSetDevice(s->device);
   lj_status st = flush_observables(s);
   if (st) return st;
-  const size_t n3 = 3 * (size_t)s->ntotal;
-  const double* src[3] = {s->x.p, s->v.p, s->f.p};
-  double* dst[3] = {pos, vel, force};
-  for (int k = 0; k < 3; ++k) {
-    if (!dst[k]) continue;
-    double* stg = s->stage.p + k * n3;
-    LJ_CUDA(s, launch_pack(src[k], stg, s->ntotal, s->npad, s->stream));
-    s->launches += 1;
-    LJ_CUDA(s, cudaMemcpyAsync(dst[k], stg, sizeof(double) * n3, cudaMemcpyDeviceToHost, s->stream));
-  }
+  st = enqueue_state_read(s, pos, vel, force);
+  if (st) return st;
   return sync_status(s);
+}
+
+// lj_get_state and lj_get_observables behind a single synchronisation.
+lj_status lj_get_state_observables(lj_system* s, double* pos, double* vel, double* force, lj_observables* out) {
+  if (!s) return LJ_ERR_INVALID;
+  cudaSetDevice(s->device);
+  lj_status st = flush_observables(s);
+  if (st) return st;
+  st = enqueue_state_read(s, pos, vel, force);
+  if (st) return st;
+  if (out)
+    LJ_CUDA(s, cudaMemcpyAsync(s->h_sc.p, s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
+  st = sync_status(s);
+  if (st) return st;
+  if (out) fill_obs(s->h_sc.p[0], out);
+  return LJ_OK;
 }
 
 lj_status lj_get_pair_sums(lj_system* s, double* e, double* w) {

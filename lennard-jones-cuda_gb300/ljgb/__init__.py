@@ -83,6 +83,7 @@ def _declare(L):
         "lj_step": (C.c_int, [_P, C.c_double, C.c_int32]),
         "lj_sync": (C.c_int, [_P]),
         "lj_get_observables": (C.c_int, [_P, C.POINTER(Observables)]),
+        "lj_get_state_observables": (C.c_int, [_P, _P, _P, _P, C.POINTER(Observables)]),
         "lj_batch_observables": (C.c_int, [_P, C.POINTER(Observables)]),
         "lj_batch_info": (C.c_int, [_P, C.POINTER(C.c_int32), _P]),
         "lj_set_recording": (C.c_int, [_P, C.c_int32]),
@@ -318,6 +319,13 @@ class System:
         """Read state into caller buffers (e.g. pinned host memory)."""
         ptr = lambda a: a.ctypes.data if a is not None else None
         self._c(load().lj_get_state(self.h, ptr(pos), ptr(vel), ptr(frc)))
+
+    def get_state_observables_into(self, pos=None, vel=None, frc=None) -> dict:
+        """State into caller buffers plus the observables, one synchronisation."""
+        ptr = lambda a: a.ctypes.data if a is not None else None
+        o = Observables()
+        self._c(load().lj_get_state_observables(self.h, ptr(pos), ptr(vel), ptr(frc), C.byref(o)))
+        return o.as_dict()
 
     def set_state_from(self, pos=None, vel=None):
         ptr = lambda a: a.ctypes.data if a is not None else None

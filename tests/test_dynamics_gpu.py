@@ -325,3 +325,35 @@ def test_device_wait_limit_reports_and_recovers(ljgb_mod):
     s.integrate(0.005, 3)
     o = s.observables()
     assert o["step"] == 5 and np.isfinite(o["U"])
+
+
+@pytest.mark.parametrize("canonical", [0, 1], ids=["evn", "tvn"])
+def test_combined_state_observables_read(ljgb_mod, canonical):
+    """lj_get_state_observables returns exactly what lj_get_state followed by
+    lj_get_observables return, on a handle whose last steps left their
+    observables pending (fused steps), after a state upload and a step."""
+    N, rho, T0 = 1000, 0.8, 1.2
+    pos, vel, L = U.lattice_state(N, rho, T0, "fcc", 0.02, seed=5)
+    a = ljgb_mod.System(n=N, density=rho, temperature=T0, canonical=canonical)
+    b = ljgb_mod.System(n=N, density=rho, temperature=T0, canonical=canonical)
+    for s in (a, b):
+        s.set_state(pos, vel)
+        s.integrate(0.005, 3)
+    pa, va, fa = (np.zeros((N, 3)) for _ in range(3))
+    oa = a.get_state_observables_into(pa, va, fa)
+    pb, vb, fb = b.get_state()
+    ob = b.observables()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+    assert oa == ob
+    # upload, one step, combined read: positions only, then nothing but the observables
+    for s in (a, b):
+        s.set_state_from(pa, va)
+        s.integrate(0.005)
+    p2 = np.zeros((N, 3))
+    oa = a.get_state_observables_into(p2, None, None)
+    pb, _, _ = b.get_state()
+    ob = b.observables()
+    assert np.array_equal(p2, pb) and oa == ob
+    assert a.get_state_observables_into() == ob
+    a.close()
+    b.close()
