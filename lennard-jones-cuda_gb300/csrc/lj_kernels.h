@@ -10,6 +10,9 @@
 namespace ljgb {
 
 constexpr int kMaxHistBins = 4096;
+// Shared-memory histogram of a pair-kernel CTA: nb 32-bit bins, rounded up to
+// 16 bytes.
+constexpr size_t hist_smem_bytes(int nb) { return (sizeof(unsigned) * (size_t)nb + 15) / 16 * 16; }
 
 // Pair-histogram request.  mode 0: r^2 bins, clamp overflow to the last bin
 // (MDSystem.cu:39); 1: r^2 bins, drop overflow (MDSystem.cpp:282-284);
@@ -52,6 +55,8 @@ int fp64_block_threads();
 int fp64_tile();
 
 cudaError_t pair_occupancy(int prec, int shape, int* blocks_per_sm);
+// Resident CTAs per SM of the MIXED histogram-only pair kernel with nb bins.
+cudaError_t pair_hist_occupancy(int shape, int nb, int* blocks_per_sm);
 cudaError_t launch_pairs(int prec, int shape, bool forces, bool hist, const PairArgs& a, int grid,
                          cudaStream_t st);
 struct FusedPairArgs;

@@ -251,6 +251,8 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
   FloatAcc acc[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) acc[c] = FloatAcc{0.f, 0.f};
+  unsigned nclamp = 0;  // HIST, clamped r^2 bins: pairs in the last bin
+  unsigned nself = 0;   // HIST: self pairs binned into bin 0
 
   // A warp whose wait times out (or that sees another warp's timeout) keeps
   // walking the tile sequence without computing, so every CTA-wide barrier
@@ -332,10 +334,28 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
         two_sum_add(acc[4], tb);
       }
       if (HIST && valid_i) {
-        for (int jj = jlo; jj < jhi; ++jj) {
-          if (j0 + jj == i_local) continue;
-          const int b = pair_bin(qi, st[jj], k2, a.hist);
-          if (b >= 0) atomicAdd(&shist[b], 1u);
+        // The self pair (separation 0) is binned with the others, into bin 0
+        // in every mode, and taken out of bin 0 once at the end: no per-pair
+        // index test.
+        const int self = i_local - j0;
+        if (self >= jlo && self < jhi) ++nself;
+        if (a.hist.mode == 0) {
+          // Clamped r^2 bins: most pairs of a box land in the last bin.  They
+          // are counted in a register and added once per warp at the end
+          // instead of by a same-address shared atomic per pair.
+          const int last_bin = a.hist.nb - 1;
+#pragma unroll 4
+          for (int jj = jlo; jj < jhi; ++jj) {
+            const int b = pair_bin(qi, st[jj], k2, a.hist);
+            if (b == last_bin) ++nclamp;
+            else atomicAdd(&shist[b], 1u);
+          }
+        } else {
+#pragma unroll 4
+          for (int jj = jlo; jj < jhi; ++jj) {
+            const int b = pair_bin(qi, st[jj], k2, a.hist);
+            if (b >= 0) atomicAdd(&shist[b], 1u);
+          }
         }
       }
     }
@@ -452,6 +472,12 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     return;
   }
   if (HIST) {
+    const unsigned wclamp = __reduce_add_sync(0xffffffffu, nclamp);
+    const unsigned wself = __reduce_add_sync(0xffffffffu, nself);
+    if (lane == 0) {
+      if (wclamp) atomicAdd(&shist[a.hist.nb - 1], wclamp);
+      if (wself) atomicSub(&shist[0], wself);
+    }
     __syncthreads();
     for (int b = tid; b < a.hist.nb; b += THREADS)
       if (shist[b]) atomicAdd(a.hist.counts + b, (unsigned long long)shist[b]);
@@ -602,8 +628,9 @@ namespace {
 
 template <int THREADS, int TILE, int STAGES, int MINB, bool FORCES, bool HIST>
 cudaError_t launch_mixed_t(const PairArgs& a, int grid, cudaStream_t st) {
-  // <= 48 KB: 16 B x STAGES x TILE staging (+ 16 KB histogram), no opt-in needed.
-  const size_t smem = sizeof(int4) * STAGES * TILE + (HIST ? sizeof(unsigned) * kMaxHistBins : 0);
+  // <= 48 KB: 16 B x STAGES x TILE staging (+ the histogram's bins, at most
+  // 16 KB), no opt-in needed.
+  const size_t smem = sizeof(int4) * STAGES * TILE + (HIST ? hist_smem_bytes(a.hist.nb) : 0);
   k_pairs_mixed<THREADS, TILE, STAGES, MINB, FORCES, HIST><<<grid, THREADS, smem, st>>>(a);
   return cudaGetLastError();
 }
@@ -621,6 +648,14 @@ cudaError_t occupancy_mixed_t(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       blocks_per_sm, k_pairs_mixed<THREADS, TILE, STAGES, MINB, true, false>, THREADS,
       sizeof(int4) * STAGES * TILE);
+}
+
+// Resident CTAs per SM of the histogram-only variant with nb bins.
+template <int THREADS, int TILE, int STAGES, int MINB>
+cudaError_t occupancy_hist_t(int nb, int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      blocks_per_sm, k_pairs_mixed<THREADS, TILE, STAGES, MINB, false, true>, THREADS,
+      sizeof(int4) * STAGES * TILE + hist_smem_bytes(nb));
 }
 
 template <int THREADS, int TILE, int STAGES>
@@ -670,6 +705,17 @@ cudaError_t pair_occupancy(int prec, int shape, int* blocks_per_sm) {
     return occupancy_mixed_t<T, TL, S, M>(blocks_per_sm);
     LJ_SHAPES(LJ_OCC_CASE)
 #undef LJ_OCC_CASE
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t pair_hist_occupancy(int shape, int nb, int* blocks_per_sm) {
+  switch (shape) {
+#define LJ_HOCC_CASE(i, T, TL, S, M) \
+  case i:                            \
+    return occupancy_hist_t<T, TL, S, M>(nb, blocks_per_sm);
+    LJ_SHAPES(LJ_HOCC_CASE)
+#undef LJ_HOCC_CASE
   }
   return cudaErrorInvalidValue;
 }

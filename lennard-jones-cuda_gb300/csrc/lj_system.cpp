@@ -137,6 +137,12 @@ struct lj_system {
   DevBuf<unsigned long long> rdf_sum;
   DevBuf<int4> qhist;
   long long rdf_samples = 0;
+  // CTA ranges of the histogram-only pair pass: the same blocks and tiles as
+  // `sched`, cut for the CTAs the histogram variant holds resident (more per
+  // SM than the force kernel: fewer registers, a small shared histogram).
+  Schedule hsched;
+  int hist_shape = -1, hist_nb = -1;
+  DevBuf<int> h_cta_tile_begin, h_cta_lo, h_cta_block, h_cta_jt;
 
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
@@ -317,6 +323,7 @@ lj_status setup_schedule(lj_system* s) {
     return fail(s, LJ_ERR_INVALID, "cannot build the pair schedule");
   s->sched = std::move(sch);
   s->BI = threads;
+  s->hist_shape = -1;  // the histogram pass re-cuts its ranges on next use
   const int nb = nblocks(s);
   LJ_CUDA(s, s->blocks.alloc(nb));
   LJ_CUDA(s, s->cta_tile_begin.alloc(s->sched.G + 1));
@@ -368,6 +375,53 @@ lj_status enqueue_pairs(lj_system* s, bool forces, bool hist, const HistArgs* h)
   if (h) p.hist = *h;
   LJ_CUDA(s, launch_pairs(s->prec, s->shape, forces, hist, p, s->sched.G, s->stream));
   s->launches += 1;
+  return LJ_OK;
+}
+
+// Arguments and grid of a histogram-only pair pass over shadow q with
+// histogram h, on `shape` (the geometry of the active schedule).  The CTA
+// ranges are cut for as many CTAs as that variant holds resident with h.nb
+// bins, and kept until the shape, the bin count or the schedule changes.
+lj_status hist_pass_args(lj_system* s, int shape, const int4* q, const HistArgs& h, PairArgs* out, int* grid) {
+  if (shape != s->hist_shape || h.nb != s->hist_nb) {
+    int per_sm = 0;
+    LJ_CUDA(s, pair_hist_occupancy(shape, h.nb, &per_sm));
+    if (per_sm < 1) return fail(s, LJ_ERR_NO_DEVICE, "histogram pair kernel cannot be resident on this device");
+    std::vector<int> n(s->nsys);
+    for (int k = 0; k < s->nsys; ++k) n[k] = s->cfg[k].n;
+    Schedule sch;
+    if (!build_schedule(n.data(), s->nsys, kShapes[shape].threads, kShapes[shape].tile, s->num_sms * per_sm,
+                        kTileOverhead, &sch))
+      return fail(s, LJ_ERR_INVALID, "cannot build the histogram schedule");
+    if (sch.BI != s->sched.BI || sch.TILE != s->sched.TILE || sch.blocks.size() != s->sched.blocks.size())
+      return fail(s, LJ_ERR_INVALID, "histogram schedule does not match the pair schedule's blocks");
+    s->hsched = std::move(sch);
+    const int G = s->hsched.G;
+    LJ_CUDA(s, s->h_cta_tile_begin.alloc(G + 1));
+    LJ_CUDA(s, s->h_cta_lo.alloc(G + 1));
+    LJ_CUDA(s, s->h_cta_block.alloc(G));
+    LJ_CUDA(s, s->h_cta_jt.alloc(G));
+    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_tile_begin.p, s->hsched.cta_tile_begin.data(), sizeof(int) * (G + 1),
+                               cudaMemcpyHostToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_lo.p, s->hsched.cta_lo.data(), sizeof(int) * (G + 1),
+                               cudaMemcpyHostToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_block.p, s->hsched.cta_block.data(), sizeof(int) * G,
+                               cudaMemcpyHostToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_jt.p, s->hsched.cta_jt.data(), sizeof(int) * G, cudaMemcpyHostToDevice,
+                               s->stream));
+    LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+    s->hist_shape = shape;
+    s->hist_nb = h.nb;
+  }
+  PairArgs p = pair_args(s);
+  p.q = q;
+  p.hist = h;
+  p.cta_tile_begin = s->h_cta_tile_begin.p;
+  p.cta_lo = s->h_cta_lo.p;
+  p.cta_block = s->h_cta_block.p;
+  p.cta_jt = s->h_cta_jt.p;
+  *out = p;
+  *grid = s->hsched.G;
   return LJ_OK;
 }
 
@@ -550,11 +604,12 @@ lj_status after_step(lj_system* s) {
     StateArgs a = state_args(s);
     a.q = s->qhist.p;
     LJ_CUDA(s, launch_quantize(a, nblocks(s), s->BI, false, s->stream));
-    PairArgs p = pair_args(s);
-    p.q = s->qhist.p;
-    p.hist = s->rdf_args;
     const int shape = (s->prec == LJ_PREC_MIXED) ? s->shape : 0;
-    LJ_CUDA(s, launch_pairs(LJ_PREC_MIXED, shape, false, true, p, s->sched.G, s->stream));
+    PairArgs p;
+    int grid = 0;
+    lj_status hst = hist_pass_args(s, shape, s->qhist.p, s->rdf_args, &p, &grid);
+    if (hst) return hst;
+    LJ_CUDA(s, launch_pairs(LJ_PREC_MIXED, shape, false, true, p, grid, s->stream));
     s->rdf_samples += 1;
     s->launches += 2;
   }
@@ -832,6 +887,10 @@ lj_status lj_destroy(lj_system* s) {
   s->counter_ring.free();
   s->rdf_sum.free();
   s->qhist.free();
+  s->h_cta_tile_begin.free();
+  s->h_cta_lo.free();
+  s->h_cta_block.free();
+  s->h_cta_jt.free();
   s->cta_lo.free();
   s->cta_block.free();
   s->cta_jt.free();
@@ -1260,16 +1319,14 @@ lj_status lj_rdf_counts(lj_system* s, int32_t mode, int32_t nbins, double width,
   }
   h.counts = s->hist.p;
   // The histogram path always runs on the fixed-point shadow.
-  const int saved = s->prec;
-  s->prec = LJ_PREC_MIXED;
-  PairArgs p = pair_args(s);
-  p.hist = h;
   // FP64 handles schedule 128-particle i-blocks and 256-record j-tiles,
   // the geometry of MIXED shape 0, so that shape reads their tables.
-  const int shape = (saved == LJ_PREC_MIXED) ? s->shape : 0;
-  const cudaError_t ce = launch_pairs(LJ_PREC_MIXED, shape, false, true, p, s->sched.G, s->stream);
-  s->prec = saved;
-  LJ_CUDA(s, ce);
+  const int shape = (s->prec == LJ_PREC_MIXED) ? s->shape : 0;
+  PairArgs p;
+  int grid = 0;
+  st = hist_pass_args(s, shape, pair_args(s).q, h, &p, &grid);
+  if (st) return st;
+  LJ_CUDA(s, launch_pairs(LJ_PREC_MIXED, shape, false, true, p, grid, s->stream));
   s->launches += 1;
   LJ_CUDA(s, cudaMemcpyAsync(counts, s->hist.p, sizeof(unsigned long long) * nbins, cudaMemcpyDeviceToHost,
                              s->stream));

@@ -35,6 +35,11 @@ def main(argv=None):
     ap.add_argument("--adjoint", type=int, default=0, metavar="K",
                     help="run the adjoint instead (EVN, FP64, checkpoints every K steps): forward + backward "
                          "of loss = <V/N + P> over --steps steps")
+    ap.add_argument("--rdf", type=int, default=-1, metavar="MODE",
+                    help="after the steps, time --calls RDF passes (0: clamped r^2 bins, 1: r^2 bins with overflow "
+                         "dropped, 2: linear r bins to L/2)")
+    ap.add_argument("--velo", action="store_true", help="after the steps, time --calls speed histograms")
+    ap.add_argument("--calls", type=int, default=20)
     a = ap.parse_args(argv)
     if a.adjoint > 0:
         adj = ljgb.Adjoint(n=a.n, density=a.rho, temperature=a.T, lattice=ljgb.LATTICE_FCC if a.fcc else
@@ -75,6 +80,22 @@ def main(argv=None):
     el = time.perf_counter() - t0
     print("n=%d steps=%d t=%.4f U/N=%.8f T=%.6f P=%.6f wall=%.3fs shape=%s" % (
         a.n, a.steps, o["t"], o["U"] / a.n, o["T"], o["P"], el, s.tune_info()["active"]))
+    if a.rdf >= 0:
+        nb, width = (200, (s.L / 2) / 200) if a.rdf == 2 else (256, ljgb.reference_rdf_dr2(a.n))
+        s.rdf_counts(a.rdf, nb, width)
+        t0 = time.perf_counter()
+        for _ in range(a.calls):
+            c = s.rdf_counts(a.rdf, nb, width)
+        ms = (time.perf_counter() - t0) * 1e3 / a.calls
+        print("rdf mode %d: %d bins, %.4f ms per call (host clock, synchronised), %d pairs counted, last bin %d" % (
+            a.rdf, nb, ms, int(c.sum()), int(c[-1])))
+    if a.velo:
+        s.velocity_counts()
+        t0 = time.perf_counter()
+        for _ in range(a.calls):
+            c = s.velocity_counts()
+        ms = (time.perf_counter() - t0) * 1e3 / a.calls
+        print("speed histogram: %.4f ms per call (host clock, synchronised), %d counted" % (ms, int(c.sum())))
     s.close()
 
 

@@ -31,6 +31,24 @@ def test_rdf_r2_counts_exact(ljgb_mod, oracle_mod, N, rho):
     assert s.rdf_counts(0, 256, dr2).sum() == N * (N - 1)
 
 
+@pytest.mark.parametrize("dr2", [0.1, 1.2])
+def test_rdf_r2_large_box_clamp_dominant_or_rare(ljgb_mod, oracle_mod, dr2):
+    """N=16384 over the whole persistent grid (ranges cut inside tiles): with
+    dr2 = 0.1 about 97% of the pairs fall in the clamp bin, with dr2 = 1.2
+    almost none; the last bin is counted per thread and added per warp."""
+    N, rho = 16384, 0.85
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.05, seed=7)
+    s = ljgb_mod.System(n=N, density=rho)
+    s.set_state(pos, vel)
+    q = oracle_mod.emu_fixed(pos, L)
+    for mode in (0, 1):
+        got = s.rdf_counts(mode, 256, dr2)
+        want = oracle_mod.emu_rdf_r2(q, k2_of(L), np.float32(1.0 / dr2), 256, mode)
+        assert np.array_equal(got, want), mode
+    assert got[:255].sum() <= N * (N - 1)
+    s.close()
+
+
 def test_rdf_linear_r_to_half_box(ljgb_mod, oracle_mod):
     """Config-1 output: a 200-bin RDF to r = L/2."""
     N, rho = 400, 0.05
