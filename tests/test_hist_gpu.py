@@ -49,6 +49,25 @@ def test_rdf_r2_large_box_clamp_dominant_or_rare(ljgb_mod, oracle_mod, dr2):
     s.close()
 
 
+def test_rdf_counts_same_on_every_shape(ljgb_mod, oracle_mod):
+    """The histogram pass cuts its own CTA ranges for the active shape's
+    blocks and tiles; changing the shape (or the bin count) re-cuts them."""
+    N, rho = 3000, 0.85
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.05, seed=9)
+    s = ljgb_mod.System(n=N, density=rho)
+    s.set_state(pos, vel)
+    q = oracle_mod.emu_fixed(pos, L)
+    dr2 = ljgb_mod.reference_rdf_dr2(N)
+    want0 = oracle_mod.emu_rdf_r2(q, k2_of(L), np.float32(1.0 / dr2), 256, 0)
+    want_wide = oracle_mod.emu_rdf_r2(q, k2_of(L), np.float32(1.0 / 0.5), 64, 1)
+    for shape in range(len(s.tune_info()["shapes"])):
+        s.set_kernel_shape(shape)
+        s.set_state(pos, vel)
+        assert np.array_equal(s.rdf_counts(0, 256, dr2), want0), shape
+        assert np.array_equal(s.rdf_counts(1, 64, 0.5), want_wide), shape
+    s.close()
+
+
 def test_rdf_linear_r_to_half_box(ljgb_mod, oracle_mod):
     """Config-1 output: a 200-bin RDF to r = L/2."""
     N, rho = 400, 0.05
