@@ -206,7 +206,11 @@ bool ensure_ctx(int n, int block_hint) {
   c.n = n;
   c.shape = shape;
   c.nb_bbox = (n + kBlk - 1) / kBlk;
-  REF_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  // A blocking stream: the reference's ABI is synchronous and its copies
+  // (copyArrayToDevice, cudaMemcpy on the legacy stream) must be ordered
+  // before this stream's kernels; a pageable cudaMemcpy can return before
+  // its DMA has landed.
+  REF_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamDefault));
   const int nb = (int)s.blocks.size();
   REF_CHECK(cudaMalloc(&c.q, sizeof(int4) * n));
   REF_CHECK(cudaMalloc(&c.sc, sizeof(DevScalars)));

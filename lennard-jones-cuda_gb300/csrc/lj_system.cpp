@@ -623,10 +623,12 @@ lj_status sync_status(lj_system* s) {
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   const int st = s->h_words.p[0];
   if (st) {
-    LJ_CUDA(s, cudaMemset(s->status.p, 0, sizeof(int)));
+    // (on the handle's stream: it is non-blocking, so a legacy-stream memset
+    // would not be ordered before the next launch)
+    LJ_CUDA(s, cudaMemsetAsync(s->status.p, 0, sizeof(int), s->stream));
     // A failed launch may leave the fused-step counters mid-count.
-    if (s->blk_cnt.p) LJ_CUDA(s, cudaMemset(s->blk_cnt.p, 0, sizeof(int) * s->blk_cnt.n));
-    if (s->glob_cnt.p) LJ_CUDA(s, cudaMemset(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n));
+    if (s->blk_cnt.p) LJ_CUDA(s, cudaMemsetAsync(s->blk_cnt.p, 0, sizeof(int) * s->blk_cnt.n, s->stream));
+    if (s->glob_cnt.p) LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n, s->stream));
     s->pred_ready = false;
     if (st & LJ_DEVFLAG_TIMEOUT)
       return fail(s, LJ_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the results of that launch are void");
@@ -1384,8 +1386,9 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
   s->counter_bins = bins;
   LJ_CUDA(s, s->dcounters.alloc(s->counters.size()));
   LJ_CUDA(s, s->counter_ring.alloc((size_t)bins * ring_steps));
-  LJ_CUDA(s, cudaMemcpy(s->dcounters.p, s->counters.data(), sizeof(CounterDev) * s->counters.size(),
-                        cudaMemcpyHostToDevice));
+  LJ_CUDA(s, cudaMemcpyAsync(s->dcounters.p, s->counters.data(), sizeof(CounterDev) * s->counters.size(),
+                             cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->counter_cap = ring_steps;
   return LJ_OK;
 }
@@ -1446,7 +1449,7 @@ lj_status lj_rdf_accumulate(lj_system* s, int32_t enable, int32_t mode, int32_t 
   if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "RDF accumulation applies to single-box handles");
   LJ_CUDA(s, s->rdf_sum.alloc(nbins));
   LJ_CUDA(s, s->qhist.alloc(s->npad));
-  LJ_CUDA(s, cudaMemset(s->rdf_sum.p, 0, sizeof(unsigned long long) * nbins));
+  LJ_CUDA(s, cudaMemsetAsync(s->rdf_sum.p, 0, sizeof(unsigned long long) * nbins, s->stream));
   HistArgs h{};
   h.mode = mode;
   h.nb = nbins;
@@ -1475,7 +1478,7 @@ lj_status lj_rdf_accumulated(lj_system* s, uint64_t* counts, int64_t* nsamples, 
     LJ_CUDA(s, cudaMemcpy(counts, s->rdf_sum.p, sizeof(unsigned long long) * s->rdf_args.nb, cudaMemcpyDeviceToHost));
   if (nsamples) *nsamples = s->rdf_samples;
   if (reset) {
-    LJ_CUDA(s, cudaMemset(s->rdf_sum.p, 0, sizeof(unsigned long long) * s->rdf_args.nb));
+    LJ_CUDA(s, cudaMemsetAsync(s->rdf_sum.p, 0, sizeof(unsigned long long) * s->rdf_args.nb, s->stream));
     s->rdf_samples = 0;
   }
   return LJ_OK;

@@ -93,12 +93,33 @@ def test_dense_liquid_configuration(ljgb_mod):
         assert om["U"] == pytest.approx(od["U"], rel=1e-6)
         assert om["P"] == pytest.approx(od["P"], rel=1e-5)
     # averages: both runs continue; trajectories decorrelate, the averages
-    # must agree within their statistical errors
-    n_avg = 400
-    mixed.set_recording(n_avg)
-    fp64.set_recording(n_avg)
-    mixed.integrate(dt, n_avg)
-    fp64.integrate(dt, n_avg)
+    # must agree within their statistical errors (U/N, P and g(r), the last
+    # summed on the device after every step, 100 linear bins to L/2, read in
+    # blocks of 50 steps for its error)
+    n_avg, nblk, nbr = 400, 8, 100
+    width = (L / 2) / nbr
+    # ordered pairs per step of an ideal gas in each shell: N rho 4/3 pi (r1^3 - r0^3)
+    edges = width * np.arange(nbr + 1)
+    ideal = N * rho * 4.0 / 3.0 * np.pi * (edges[1:] ** 3 - edges[:-1] ** 3)
+    g = {}
+    for name, s in (("mixed", mixed), ("fp64", fp64)):
+        s.set_recording(n_avg)
+        s.rdf_accumulate(True, mode=ljgb_mod.RDF_R_LINEAR, nbins=nbr, width=width)
+        blocks = []
+        for _ in range(nblk):
+            s.integrate(dt, n_avg // nblk)
+            c, ns = s.rdf_accumulated(reset=True)
+            assert ns == n_avg // nblk
+            blocks.append(c.astype(np.float64) / ns / ideal)
+        g[name] = np.array(blocks)
+        s.rdf_accumulate(False)
+    gm, gd = g["mixed"].mean(0), g["fp64"].mean(0)
+    sem = np.hypot(g["mixed"].std(0, ddof=1), g["fp64"].std(0, ddof=1)) / np.sqrt(nblk)
+    dev = np.abs(gm - gd) / (sem + 2e-3 * gd.max())
+    print("dense liquid g(r) over %d steps: first peak g=%.4f at r=%.3f, max |mixed - fp64| / error %.2f "
+          "(max |dg| %.2e)" % (n_avg, gd.max(), (gd.argmax() + 0.5) * width, dev.max(), np.abs(gm - gd).max()))
+    assert 2.0 < gd.max() < 4.0 and abs(gd[-10:].mean() - 1.0) < 0.05
+    assert dev.max() < 6
     res = {}
     for name, s in (("mixed", mixed), ("fp64", fp64)):
         rec = s.records()
