@@ -302,12 +302,20 @@ def extra_configs(torch, ljgb, oracle, dev, flush, peak):
     steps = 20
     ms, _, launches = timed_steps(torch, b, steps, 3, flush, dt=0.004)
     pairs = float(sum(c.n * (c.n - 1) for c in cfgs))
+    # per-replica U/N and P, averaged over every step the replicas ran (the
+    # device's running sums, MDSystem.cpp:355-358)
+    obs = b.batch_observables()
+    per_replica = {
+        "steps_averaged": int(obs[0]["av_iters"]),
+        "n": [int(c.n) for c in cfgs],
+        "U_per_N": [float("%.6g" % (o["av_U_tot"] / max(1, o["av_iters"]) / c.n)) for o, c in zip(obs, cfgs)],
+        "P": [float("%.6g" % (o["av_p_tot"] / max(1, o["av_iters"]))) for o in obs]}
     out["batch_256"] = {
         "workload": "256 replicas, N U[200,4000) (sum %d), rho* U[0.01,1.1], T* U[0.7,2.0], half walls, TVN, "
                     "dt=0.004" % sum(c.n for c in cfgs),
         "ms_per_step": ms / steps, "steps_per_s": 1e3 * steps / ms, "replica_steps_per_s": 256e3 * steps / ms,
         "pair_interactions_per_s": pairs * steps / (ms * 1e-3), "gpu_launches_per_step": launches / steps,
-        "l2": "flushed before every timed step"}
+        "l2": "flushed before every timed step", "per_replica": per_replica}
     b.close()
     # one large box: N = 262144, rho* = 1.1, T* = 1.0, FCC + 0.01, dt = 0.004, TVN
     n = 262144

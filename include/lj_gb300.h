@@ -82,7 +82,8 @@ typedef struct {
   uint64_t seed;        /* seed of the initial-condition generator */
   int32_t block_hint;   /* CUDABlockSize (MDSystem.h:29); 0 = use the autotuned shape */
   int32_t device;       /* CUDA device ordinal */
-  int32_t autotune;     /* 1: time the kernel shapes on first use and keep the fastest */
+  int32_t autotune;     /* reserved (kept for the layout); shapes and the split cap are
+                           timed when the caller runs lj_autotune */
 } lj_config;
 
 /* Thermodynamic state after the last force evaluation / step.  Same
@@ -93,7 +94,9 @@ typedef struct {
   double t;          /* simulation time (MDSystem.h:80) */
   double K, V, T, P, U;
   double W;          /* virial sum over ordered pairs, r_ij . f_ij */
-  double Pshear;     /* off-diagonal stress (0 unless shear accumulation is enabled) */
+  double Pshear;     /* off-diagonal stress: always 0.  The reference computes it on its
+                        CPU path only (MDSystem.cpp:259, 299, 309, 335); its GPU path
+                        never updates it. */
   double Tkin_tvn;   /* TVN: kinetic temperature of the half-kicked velocities, else 0 */
   double av_U_tot, av_T_tot, av_p_tot; /* running sums, MDSystem.h:98 */
   int64_t av_iters;  /* MDSystem.h:99 */
@@ -102,7 +105,7 @@ typedef struct {
 
 /* Fills *cfg with MDSystemConfiguration's defaults (MDSystem.h:32-40):
  * N=128, T0=1.5, rho=0.2, EVN, periodic; plus eps=sigma=1, SC lattice,
- * no jitter, seed 1, mixed precision, device 0, autotune on. */
+ * no jitter, seed 1, mixed precision, device 0, autotune field 1. */
 lj_status lj_config_default(lj_config* cfg);
 
 /* MDSystem::MDSystem / Reinitialize (MDSystem.cpp:55-114): allocates the box
@@ -211,6 +214,17 @@ lj_status lj_set_kernel_shape(lj_system* sys, int32_t shape);
  * thread and j-tile length; *active = shape in use. */
 lj_status lj_tune_info(lj_system* sys, int32_t* nshapes, int32_t* active, int32_t k,
                        int32_t* threads, int32_t* ipt, int32_t* tile);
+
+/* Threads per particle.  The reference gives each particle one thread over
+ * all j (MDSystem.cu:74-111, 113-138); here an i-block's j range is cut over
+ * up to `cap` CTAs, i.e. up to `cap` threads per particle, each summing a
+ * j sub-range into its own partial segment.  lj_autotune searches the cap
+ * together with the shape (caps 1..32 that change the grid); lj_set_split_cap
+ * fixes it (0: back to the default 8, searched again by lj_autotune).
+ * lj_split_info reports the cap in use, the CTAs of the persistent grid and
+ * the most segments any i-block has. */
+lj_status lj_set_split_cap(lj_system* sys, int32_t cap);
+lj_status lj_split_info(lj_system* sys, int32_t* cap, int32_t* ctas, int32_t* max_segments);
 
 /* Device-time profiling.  When enabled, each pair-kernel launch inside
  * lj_step / lj_compute_forces is bracketed by CUDA events on the handle's

@@ -94,6 +94,10 @@ struct lj_system {
   // kernel shape / schedule
   int shape = 0;        // index into kShapes (MIXED)
   int forced_shape = -1;
+  // Threads per particle: the most CTAs (j-range splits) one i-block is cut
+  // into, each giving its particles one thread over part of the j range.
+  int split_cap = kMaxSegmentsPerBlock;
+  int forced_split = 0;  // > 0: set by lj_set_split_cap, kept by the autotuner
   bool tuned = false;
   Schedule sched;
   int BI = 128;
@@ -317,7 +321,7 @@ lj_status setup_schedule(lj_system* s) {
   // occupancy / 128 is unaffected).
   long long nbt = 0;
   for (int k = 0; k < s->nsys; ++k) nbt += (n[k] + threads - 1) / threads;
-  const int G = (int)std::min<long long>((long long)s->num_sms * blocks_per_sm, nbt * kMaxSegmentsPerBlock);
+  const int G = (int)std::min<long long>((long long)s->num_sms * blocks_per_sm, nbt * s->split_cap);
   Schedule sch;
   if (!build_schedule(n.data(), s->nsys, threads, tile, G, kTileOverhead, &sch))
     return fail(s, LJ_ERR_INVALID, "cannot build the pair schedule");
@@ -1542,6 +1546,31 @@ lj_status lj_set_kernel_shape(lj_system* s, int32_t shape) {
   return enqueue_compute_forces(s);
 }
 
+lj_status lj_set_split_cap(lj_system* s, int32_t cap) {
+  if (!s) return LJ_ERR_INVALID;
+  if (cap < 0 || cap > 1024) return fail(s, LJ_ERR_INVALID, "split cap %d out of range [0, 1024]", cap);
+  cudaSetDevice(s->device);
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->forced_split = cap;
+  s->split_cap = cap > 0 ? cap : kMaxSegmentsPerBlock;
+  lj_status st = setup_schedule(s);
+  if (st) return st;
+  // The partial segments were re-cut: rebuild the per-block sums.
+  return enqueue_compute_forces(s);
+}
+
+lj_status lj_split_info(lj_system* s, int32_t* cap, int32_t* ctas, int32_t* max_segments) {
+  if (!s) return LJ_ERR_INVALID;
+  if (cap) *cap = s->split_cap;
+  if (ctas) *ctas = s->sched.G;
+  if (max_segments) {
+    int m = 0;
+    for (const BlockInfo& b : s->sched.blocks) m = std::max(m, b.seg_count);
+    *max_segments = m;
+  }
+  return LJ_OK;
+}
+
 lj_status lj_autotune(lj_system* s) {
   if (!s) return LJ_ERR_INVALID;
   if (s->prec == LJ_PREC_FP64) return LJ_OK;  // one FP64 shape
@@ -1595,30 +1624,44 @@ lj_status lj_autotune(lj_system* s) {
   cudaEvent_t e0, e1;
   LJ_CUDA(s, cudaEventCreate(&e0));
   LJ_CUDA(s, cudaEventCreate(&e1));
-  int best = 0;
+  // Two dimensions: the CTA shape (threads, j-tile, stages) and the threads
+  // per particle (the split cap: CTAs an i-block may be cut into).  A cap
+  // only matters while it keeps the grid below SMs x resident CTAs; larger
+  // caps give the same schedule and are skipped.
+  static const int kSplitCaps[] = {1, 2, 4, 8, 16, 32};
+  int best = 0, best_split = s->split_cap;
   float best_ms = 1e30f;
   for (int k = 0; k < kNumShapes; ++k) {
-    s->shape = k;
-    if ((st = setup_schedule(s))) return st;
-    if ((st = restore())) return st;
-    if ((st = enqueue_compute_forces(s))) return st;
-    if ((st = lj_step(s, dt, 2))) return st;
-    LJ_CUDA(s, cudaEventRecord(e0, s->stream));
-    const int reps = 6;
-    if ((st = lj_step(s, dt, reps))) return st;
-    LJ_CUDA(s, cudaEventRecord(e1, s->stream));
-    LJ_CUDA(s, cudaEventSynchronize(e1));
-    float ms = 0;
-    LJ_CUDA(s, cudaEventElapsedTime(&ms, e0, e1));
-    if ((st = check_status(s))) return st;
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = k;
+    int prev_G = -1;
+    for (int cap : kSplitCaps) {
+      if (s->forced_split > 0 && cap != kSplitCaps[0]) break;
+      s->shape = k;
+      s->split_cap = s->forced_split > 0 ? s->forced_split : cap;
+      if ((st = setup_schedule(s))) return st;
+      if (s->sched.G == prev_G) break;
+      prev_G = s->sched.G;
+      if ((st = restore())) return st;
+      if ((st = enqueue_compute_forces(s))) return st;
+      if ((st = lj_step(s, dt, 2))) return st;
+      LJ_CUDA(s, cudaEventRecord(e0, s->stream));
+      const int reps = 6;
+      if ((st = lj_step(s, dt, reps))) return st;
+      LJ_CUDA(s, cudaEventRecord(e1, s->stream));
+      LJ_CUDA(s, cudaEventSynchronize(e1));
+      float ms = 0;
+      LJ_CUDA(s, cudaEventElapsedTime(&ms, e0, e1));
+      if ((st = check_status(s))) return st;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = k;
+        best_split = s->split_cap;
+      }
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   s->shape = best;
+  s->split_cap = best_split;
   s->tuned = true;
   s->profiling = was_profiling;
   if ((st = setup_schedule(s))) return st;

@@ -99,6 +99,8 @@ def _declare(L):
         "lj_reference_rdf_dr2": (C.c_float, [C.c_int32]),
         "lj_velocity_counts": (C.c_int, [_P, C.c_double, C.c_int32, _P]),
         "lj_autotune": (C.c_int, [_P]),
+        "lj_set_split_cap": (C.c_int, [_P, C.c_int32]),
+        "lj_split_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
         "lj_set_kernel_shape": (C.c_int, [_P, C.c_int32]),
         "lj_tune_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
@@ -455,7 +457,15 @@ class System:
             th, ipt, tl = C.c_int32(), C.c_int32(), C.c_int32()
             self._c(L.lj_tune_info(self.h, None, None, k, C.byref(th), C.byref(ipt), C.byref(tl)))
             shapes.append(dict(threads=th.value, ipt=ipt.value, tile=tl.value))
-        return dict(active=act.value, shapes=shapes)
+        cap, ctas, segs = C.c_int32(), C.c_int32(), C.c_int32()
+        self._c(L.lj_split_info(self.h, C.byref(cap), C.byref(ctas), C.byref(segs)))
+        return dict(active=act.value, shapes=shapes, split_cap=cap.value, ctas=ctas.value,
+                    max_segments=segs.value)
+
+    def set_split_cap(self, cap: int):
+        """Most CTAs (threads per particle) an i-block's j range is cut over;
+        0 restores the default, which lj_autotune searches."""
+        self._c(load().lj_set_split_cap(self.h, int(cap)))
 
     def profile(self, on: bool):
         self._c(load().lj_profile_enable(self.h, int(bool(on))))

@@ -176,3 +176,39 @@ def test_fp64_and_mixed_agree_on_observables(ljgb_mod):
         out.append(s.observables())
     for k in ("K", "V", "W", "P", "U"):
         assert out[0][k] == pytest.approx(out[1][k], rel=1e-6), k
+
+
+def test_threads_per_particle_split_cap(ljgb_mod, oracle_mod):
+    """The i-block j-range split (threads per particle) is searched by the
+    autotuner and can be fixed; forces stay within the gate for every cap and
+    the dynamics agree across caps."""
+    N, rho = 1500, 0.85
+    pos, vel, L = U.lattice_state(N, rho, 1.0, "fcc", 0.02, seed=21)
+    ref = oracle_mod.f64_forces(pos, L, True, nthreads=4)
+    obs = {}
+    for cap in (1, 3, 32, 0):
+        s = ljgb_mod.System(n=N, density=rho, temperature=1.0, canonical=1)
+        s.set_split_cap(cap)
+        s.set_state(pos, vel)
+        s.calculate_forces()
+        info = s.tune_info()
+        assert info["split_cap"] == (cap if cap > 0 else 8)
+        assert 1 <= info["max_segments"] <= info["split_cap"]
+        _, _, F = s.get_state()
+        err = U.force_errors(F, ref["F"])
+        assert err["gate_max"] <= 1e-5, (cap, err)
+        s.integrate(0.005, 5)
+        obs[cap] = s.observables()
+        s.close()
+    for cap in (1, 3, 32):
+        assert obs[cap]["U"] == pytest.approx(obs[0]["U"], rel=1e-7)
+    # the autotuner picks a shape and a cap among the searched ones
+    s = ljgb_mod.System(n=N, density=rho, temperature=1.0, canonical=1)
+    s.autotune()
+    info = s.tune_info()
+    assert info["split_cap"] in (1, 2, 4, 8, 16, 32)
+    assert info["ctas"] >= 1
+    s.set_split_cap(2)
+    s.autotune()  # a fixed cap is kept
+    assert s.tune_info()["split_cap"] == 2
+    s.close()
