@@ -239,7 +239,9 @@ std::mutex g_static_mu;
 unsigned char* g_static_ptr[kMaxDevices] = {nullptr};
 int g_static_plan_n[kMaxDevices];
 int g_static_sms[kMaxDevices];
-StaticPlan g_static_plan;
+int g_static_G[kMaxDevices];        // launch sizes of the plan each device holds
+int g_static_nblocks[kMaxDevices];
+StaticPlan g_static_plan;            // host staging of the plan being uploaded
 
 int static_fail(int code, const char* msg) {
   std::fprintf(stderr, "lj_forces_static: %s\n", msg);
@@ -308,8 +310,10 @@ extern "C" lj_status lj_forces_static(const float* pos4, float* force4, double* 
         (e = cudaStreamSynchronize(st)))
       return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
     g_static_plan_n[dev] = n;
+    g_static_G[dev] = p.G;
+    g_static_nblocks[dev] = p.nblocks;
   }
-  const StaticPlan& p = g_static_plan;
+  const int G = g_static_G[dev], nblocks = g_static_nblocks[dev];
   const float4* pos = reinterpret_cast<const float4*>(pos4);
   const int nbb = (n + kBboxThreads - 1) / kBboxThreads;
   if (!periodic) k_static_bbox<<<nbb, kBboxThreads, 0, st>>>(pos, n, blk);
@@ -326,10 +330,10 @@ extern "C" lj_status lj_forces_static(const float* pos4, float* force4, double* 
   a.partial = partial;
   a.status = status;
   a.hist = HistArgs{0, 1, 1.0f, 0.0f, nullptr};
-  if ((e = launch_pairs(0, kShape, true, false, a, p.G, st)) != cudaSuccess)
+  if ((e = launch_pairs(0, kShape, true, false, a, G, st)) != cudaSuccess)
     return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
-  k_static_reduce<<<p.nblocks, kBI, 0, st>>>(partial, blocks, sc, reinterpret_cast<float4*>(force4), blk);
-  k_static_sums<<<1, 256, 0, st>>>(blk, p.nblocks, dsums);
+  k_static_reduce<<<nblocks, kBI, 0, st>>>(partial, blocks, sc, reinterpret_cast<float4*>(force4), blk);
+  k_static_sums<<<1, 256, 0, st>>>(blk, nblocks, dsums);
   if ((e = cudaGetLastError()) != cudaSuccess) return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
   int hs = 0;
   double hsum[2] = {0, 0};
