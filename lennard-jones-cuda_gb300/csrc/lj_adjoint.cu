@@ -355,7 +355,8 @@ lj_status lj_adjoint_create(const lj_config* cfg, int32_t checkpoint_every, lj_a
     lj_adjoint_destroy(a);
     return st;
   };
-  if (cudaSetDevice(a->device) != cudaSuccess) return bail(LJ_ERR_NO_DEVICE);
+  DeviceGuard device_guard(a->device);
+  if (!device_guard.ok()) return bail(LJ_ERR_NO_DEVICE);
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, a->device) != cudaSuccess)
     return bail(LJ_ERR_NO_DEVICE);
@@ -381,7 +382,7 @@ lj_status lj_adjoint_create(const lj_config* cfg, int32_t checkpoint_every, lj_a
 
 lj_status lj_adjoint_destroy(lj_adjoint* a) {
   if (!a) return LJ_OK;
-  cudaSetDevice(a->device);
+  DeviceGuard device_guard(a->device);
   if (a->stream) cudaStreamSynchronize(a->stream);
   for (DBuf<double>* b : {&a->x, &a->v, &a->f, &a->x0, &a->v0, &a->part, &a->ckpt, &a->seg, &a->Xb, &a->bb, &a->z,
                           &a->blk, &a->hostio})
@@ -396,7 +397,7 @@ const char* lj_adjoint_last_error(const lj_adjoint* a) { return a ? a->err.c_str
 lj_status lj_adjoint_set_state(lj_adjoint* a, const double* pos, const double* vel) {
   if (!a) return LJ_ERR_INVALID;
   if (!pos || !vel) return afail(a, LJ_ERR_INVALID, "pos and vel must be non-NULL");
-  cudaSetDevice(a->device);
+  DeviceGuard device_guard(a->device);
   const size_t bytes = sizeof(double) * 3 * a->n;
   const int g = (a->n + 255) / 256;
   ADJ_CUDA(a, cudaMemcpyAsync(a->hostio.p, pos, bytes, cudaMemcpyHostToDevice, a->stream));
@@ -424,7 +425,7 @@ lj_status lj_adjoint_forward(lj_adjoint* a, double dt, int32_t nsteps, double* l
   if (!a) return LJ_ERR_INVALID;
   if (!(dt > 0) || !std::isfinite(dt)) return afail(a, LJ_ERR_INVALID, "dt must be > 0");
   if (nsteps < 1) return afail(a, LJ_ERR_INVALID, "nsteps must be >= 1");
-  cudaSetDevice(a->device);
+  DeviceGuard device_guard(a->device);
   a->dt = dt;
   a->S = nsteps;
   a->have_forward = false;
@@ -487,7 +488,7 @@ lj_status lj_adjoint_observables(lj_adjoint* a, double* K, double* V, double* W,
 lj_status lj_adjoint_backward(lj_adjoint* a, double* d_epsilon, double* d_sigma, double* d_pos, double* d_vel) {
   if (!a) return LJ_ERR_INVALID;
   if (!a->have_forward) return afail(a, LJ_ERR_INVALID, "lj_adjoint_backward needs a forward pass first");
-  cudaSetDevice(a->device);
+  DeviceGuard device_guard(a->device);
   const size_t s3 = xyz(a);
   const int S = a->S, k = a->every, J = (S + k - 1) / k;
   const double N = (double)a->n, dt = a->dt, rho = a->rho;

@@ -134,6 +134,7 @@ __global__ void k_ref_pressure(const double* blk, int nb, float* out) {
 }
 
 struct CompatCtx {
+  int device = -1;  // the device that holds the buffers below
   int n = 0;
   int shape = -1;
   int nb_bbox = 0;
@@ -187,10 +188,17 @@ bool ensure_ctx(int n, int block_hint) {
   int shape = 0;
   for (int k = 0; k < kNumShapes; ++k)
     if (std::abs(kShapes[k].threads - block_hint) < std::abs(kShapes[shape].threads - block_hint)) shape = k;
-  if (g_ctx.n == n && g_ctx.shape == shape && g_ctx.stream) return true;
-  g_ctx.release();
   int dev = 0, sms = 0, per_sm = 0;
   REF_CHECK(cudaGetDevice(&dev));
+  if (g_ctx.n == n && g_ctx.shape == shape && g_ctx.stream && g_ctx.device == dev) return true;
+  if (g_ctx.stream && g_ctx.device != dev) {
+    // The caller switched devices: free the old buffers on their own device.
+    REF_CHECK(cudaSetDevice(g_ctx.device));
+    g_ctx.release();
+    REF_CHECK(cudaSetDevice(dev));
+  } else {
+    g_ctx.release();
+  }
   REF_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   REF_CHECK(pair_occupancy(0, shape, &per_sm));
   Schedule s;
@@ -203,6 +211,7 @@ bool ensure_ctx(int n, int block_hint) {
     return false;
   }
   CompatCtx c;
+  c.device = dev;
   c.n = n;
   c.shape = shape;
   c.nb_bbox = (n + kBlk - 1) / kBlk;

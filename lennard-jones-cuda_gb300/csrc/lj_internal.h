@@ -1,9 +1,36 @@
 // lj_internal.h -- host/device shared structures of the LJ GB300 library.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 namespace ljgb {
+
+// Makes `device` current for the lifetime of the guard and puts the caller's
+// device back afterwards: an lj_* call on a handle leaves the calling
+// thread's current device as it found it.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+    if (prev_ != device) {
+      err_ = cudaSetDevice(device);
+      switched_ = err_ == cudaSuccess && prev_ >= 0;
+    }
+  }
+  ~DeviceGuard() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  bool ok() const { return err_ == cudaSuccess; }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+ private:
+  int prev_ = -1;
+  bool switched_ = false;
+  cudaError_t err_ = cudaSuccess;
+};
 
 // Device-side status flags (DevScalars::status).
 enum : int {

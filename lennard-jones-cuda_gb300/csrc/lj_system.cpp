@@ -781,7 +781,8 @@ lj_status create_impl(const lj_config* cfgs, int nsys, lj_system** out) {
     lj_destroy(s);
     return st;
   };
-  if (cudaSetDevice(s->device) != cudaSuccess) return bail(fail(s, LJ_ERR_CUDA, "cudaSetDevice failed"));
+  DeviceGuard device_guard(s->device);
+  if (!device_guard.ok()) return bail(fail(s, LJ_ERR_CUDA, "cudaSetDevice failed"));
   if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(s, LJ_ERR_CUDA, "cudaStreamCreate failed"));
   s->stream = s->own_stream;
@@ -868,7 +869,7 @@ lj_status lj_batch_create(const lj_config* cfgs, int32_t nsys, lj_system** out) 
 
 lj_status lj_destroy(lj_system* s) {
   if (!s) return LJ_OK;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   clear_graphs(s);
   for (auto e : s->ev_pool) cudaEventDestroy(e);
@@ -945,7 +946,7 @@ lj_status lj_reinitialize(lj_system* s, const lj_config* cfg) {
 lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
   if (!s) return LJ_ERR_INVALID;
   if (!pos && !vel) return LJ_OK;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status fst = flush_observables(s);
   if (fst) return fst;
   s->pred_ready = false;
@@ -1009,7 +1010,7 @@ static lj_status enqueue_state_read(lj_system* s, double* pos, double* vel, doub
 // synchronisation, which also reports the device status.
 lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = flush_observables(s);
   if (st) return st;
   st = enqueue_state_read(s, pos, vel, force);
@@ -1020,7 +1021,7 @@ lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
 // lj_get_state and lj_get_observables behind a single synchronisation.
 lj_status lj_get_state_observables(lj_system* s, double* pos, double* vel, double* force, lj_observables* out) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = flush_observables(s);
   if (st) return st;
   st = enqueue_state_read(s, pos, vel, force);
@@ -1035,7 +1036,7 @@ lj_status lj_get_state_observables(lj_system* s, double* pos, double* vel, doubl
 
 lj_status lj_get_pair_sums(lj_system* s, double* e, double* w) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   if (e) LJ_CUDA(s, cudaMemcpy(e, s->e.p, sizeof(double) * s->ntotal, cudaMemcpyDeviceToHost));
@@ -1045,7 +1046,7 @@ lj_status lj_get_pair_sums(lj_system* s, double* e, double* w) {
 
 lj_status lj_compute_forces(lj_system* s) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   return enqueue_compute_forces(s);
 }
 
@@ -1054,7 +1055,7 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
   if (nsteps < 0) return fail(s, LJ_ERR_INVALID, "nsteps must be >= 0");
   if (!(dt > 0) || !std::isfinite(dt)) return fail(s, LJ_ERR_INVALID, "dt must be > 0");
   if (nsteps == 0) return LJ_OK;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   bool changed = false;
   for (auto& b : s->boxes)
     if (b.dt != dt) {
@@ -1102,13 +1103,13 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
 
 lj_status lj_sync(lj_system* s) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   return check_status(s);
 }
 
 lj_status lj_get_observables(lj_system* s, lj_observables* out) {
   if (!s || !out) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = fetch_scalars(s);
   if (st) return st;
   fill_obs(s->h_sc.p[0], out);
@@ -1117,7 +1118,7 @@ lj_status lj_get_observables(lj_system* s, lj_observables* out) {
 
 lj_status lj_batch_observables(lj_system* s, lj_observables* out) {
   if (!s || !out) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = fetch_scalars(s);
   if (st) return st;
   for (int k = 0; k < s->nsys; ++k) fill_obs(s->h_sc.p[k], out + k);
@@ -1126,7 +1127,7 @@ lj_status lj_batch_observables(lj_system* s, lj_observables* out) {
 
 lj_status lj_set_recording(lj_system* s, int32_t cap) {
   if (!s || cap < 0) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   const DevRecord* old_records = s->records.p;
   const int old_cap = s->rec_cap;
@@ -1145,7 +1146,7 @@ lj_status lj_set_recording(lj_system* s, int32_t cap) {
 
 lj_status lj_get_records(lj_system* s, lj_observables* out, int32_t max, int32_t* count) {
   if (!s || !count || max < 0) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   *count = 0;
@@ -1182,7 +1183,7 @@ lj_status lj_get_records(lj_system* s, lj_observables* out, int32_t max, int32_t
 
 lj_status lj_reset_averaging(lj_system* s) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   std::vector<DevScalars> sc;
   lj_status st = read_scalars(s, sc);
   if (st) return st;
@@ -1195,7 +1196,7 @@ lj_status lj_reset_averaging(lj_system* s) {
 
 lj_status lj_set_canonical(lj_system* s, int32_t canonical) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   for (int k = 0; k < s->nsys; ++k) {
     s->cfg[k].canonical = canonical ? 1 : 0;
     s->boxes[k].canonical = canonical ? 1 : 0;
@@ -1206,7 +1207,7 @@ lj_status lj_set_canonical(lj_system* s, int32_t canonical) {
 lj_status lj_set_boundary(lj_system* s, int32_t bc) {
   if (!s) return LJ_ERR_INVALID;
   if (bc < 0 || bc > 2) return fail(s, LJ_ERR_INVALID, "boundary must be 0, 1 or 2");
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   for (int k = 0; k < s->nsys; ++k) {
     s->cfg[k].boundary = bc;
     s->boxes[k].bc = bc;
@@ -1219,7 +1220,7 @@ lj_status lj_set_boundary(lj_system* s, int32_t bc) {
 
 lj_status lj_set_temperature(lj_system* s, double T0) {
   if (!s || !(T0 >= 0)) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   for (int k = 0; k < s->nsys; ++k) {
     s->cfg[k].temperature = T0;
     s->boxes[k].T0 = T0;
@@ -1229,7 +1230,7 @@ lj_status lj_set_temperature(lj_system* s, double T0) {
 
 lj_status lj_set_time(lj_system* s, double t) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   std::vector<DevScalars> sc;
   lj_status st = read_scalars(s, sc);
   if (st) return st;
@@ -1240,7 +1241,7 @@ lj_status lj_set_time(lj_system* s, double t) {
 lj_status lj_renormalize_velocities(lj_system* s, int32_t recalc) {
   if (!s) return LJ_ERR_INVALID;
   if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "renormalization applies to single-box handles");
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   std::vector<DevScalars> sc;
@@ -1273,7 +1274,7 @@ lj_status lj_renormalize_velocities(lj_system* s, int32_t recalc) {
 lj_status lj_renormalize_velocities_to_energy(lj_system* s, double ust) {
   if (!s) return LJ_ERR_INVALID;
   if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "renormalization applies to single-box handles");
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   std::vector<DevScalars> sc;
@@ -1306,7 +1307,7 @@ lj_status lj_rdf_counts(lj_system* s, int32_t mode, int32_t nbins, double width,
   if (nbins < 1 || nbins > kMaxHistBins) return fail(s, LJ_ERR_INVALID, "nbins must be in [1, %d]", kMaxHistBins);
   if (!(width > 0)) return fail(s, LJ_ERR_INVALID, "bin width must be > 0");
   if (s->nsys != 1) return fail(s, LJ_ERR_UNSUPPORTED, "RDF counts apply to single-box handles");
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = enqueue_frame_all(s);
   if (st) return st;
   LJ_CUDA(s, cudaMemsetAsync(s->hist.p, 0, sizeof(unsigned long long) * nbins, s->stream));
@@ -1343,7 +1344,7 @@ lj_status lj_velocity_counts(lj_system* s, double step, int32_t nbins, uint64_t*
   if (!s || !counts) return LJ_ERR_INVALID;
   if (nbins < 1 || nbins > kMaxHistBins) return fail(s, LJ_ERR_INVALID, "nbins must be in [1, %d]", kMaxHistBins);
   if (!(step > 0)) return fail(s, LJ_ERR_INVALID, "step must be > 0");
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaMemsetAsync(s->hist.p, 0, sizeof(unsigned long long) * nbins, s->stream));
   StateArgs a = state_args(s);
   LJ_CUDA(s, launch_velocity_hist(a, nblocks(s), s->BI, step, nbins, s->hist.p, s->stream));
@@ -1355,7 +1356,7 @@ lj_status lj_velocity_counts(lj_system* s, double step, int32_t nbins, uint64_t*
 
 lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_t ncounters, int32_t ring_steps) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->counters.clear();
   s->counter_cap = 0;
@@ -1407,7 +1408,7 @@ lj_status lj_counters_set_interval(lj_system* s, int32_t every) {
 
 lj_status lj_counters_read(lj_system* s, int32_t* counts, int32_t max_steps, int32_t* nsteps) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   const long long avail = s->counter_head - s->counter_tail;
@@ -1442,7 +1443,7 @@ lj_status lj_counters_read(lj_system* s, int32_t* counts, int32_t max_steps, int
 
 lj_status lj_rdf_accumulate(lj_system* s, int32_t enable, int32_t mode, int32_t nbins, double width) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->rdf_acc = false;
   s->rdf_samples = 0;
@@ -1474,7 +1475,7 @@ lj_status lj_rdf_accumulate(lj_system* s, int32_t enable, int32_t mode, int32_t 
 
 lj_status lj_rdf_accumulated(lj_system* s, uint64_t* counts, int64_t* nsamples, int32_t reset) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   if (!s->rdf_acc) return fail(s, LJ_ERR_INVALID, "RDF accumulation is not enabled");
@@ -1496,7 +1497,7 @@ lj_status lj_render(lj_system* s, int32_t box, int32_t axis, int32_t width, int3
   if (width < 1 || height < 1 || (long long)width * height > (1ll << 26))
     return fail(s, LJ_ERR_INVALID, "image size must be 1 .. 2^26 pixels");
   if (!(radius > 0)) return fail(s, LJ_ERR_INVALID, "radius must be > 0");
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   const size_t npix = (size_t)width * height;
@@ -1536,7 +1537,7 @@ lj_status lj_set_kernel_shape(lj_system* s, int32_t shape) {
   if (!s) return LJ_ERR_INVALID;
   if (shape < -1 || shape >= kNumShapes) return fail(s, LJ_ERR_INVALID, "shape %d out of range", shape);
   if (s->prec == LJ_PREC_FP64) return LJ_OK;  // one FP64 shape
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->forced_shape = shape;
   s->shape = shape < 0 ? 0 : shape;
@@ -1549,7 +1550,7 @@ lj_status lj_set_kernel_shape(lj_system* s, int32_t shape) {
 lj_status lj_set_split_cap(lj_system* s, int32_t cap) {
   if (!s) return LJ_ERR_INVALID;
   if (cap < 0 || cap > 1024) return fail(s, LJ_ERR_INVALID, "split cap %d out of range [0, 1024]", cap);
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->forced_split = cap;
   s->split_cap = cap > 0 ? cap : kMaxSegmentsPerBlock;
@@ -1574,7 +1575,7 @@ lj_status lj_split_info(lj_system* s, int32_t* cap, int32_t* ctas, int32_t* max_
 lj_status lj_autotune(lj_system* s) {
   if (!s) return LJ_ERR_INVALID;
   if (s->prec == LJ_PREC_FP64) return LJ_OK;  // one FP64 shape
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
   // Every shape is timed on whole steps of this very system (the fused step
@@ -1676,7 +1677,7 @@ lj_status lj_autotune(lj_system* s) {
 
 lj_status lj_selftest_device_timeout(lj_system* s) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);  // earlier errors are reported as such
   if (st) return st;
   LJ_CUDA(s, launch_selftest_wait(s->status.p, s->stream));
@@ -1689,7 +1690,7 @@ lj_status lj_selftest_device_timeout(lj_system* s) {
 
 lj_status lj_profile_enable(lj_system* s, int32_t on) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->profiling = on != 0;
   s->ev_used = 0;
@@ -1700,7 +1701,7 @@ lj_status lj_profile_enable(lj_system* s, int32_t on) {
 
 lj_status lj_profile_read(lj_system* s, int64_t* pair_launches, double* pair_ms, int64_t* steps, double* step_ms) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   // Events are used four per step: step start, pair start, pair end, step end.
   for (size_t k = 0; k + 3 < s->ev_used; k += 4) {
@@ -1728,7 +1729,7 @@ lj_status lj_get_stream(lj_system* s, void** stream) {
 
 lj_status lj_set_stream(lj_system* s, void* stream) {
   if (!s) return LJ_ERR_INVALID;
-  cudaSetDevice(s->device);
+  DeviceGuard device_guard(s->device);
   lj_status st = flush_observables(s);
   if (st) return st;
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
