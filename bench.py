@@ -286,10 +286,7 @@ def batch_configs(ljgb, seed=3, k=256):
     """The batched-replicas configuration: 256 boxes, N in [200, 4000),
     rho* in [0.01, 1.1], T* in [0.7, 2.0], half periodic and half hard-wall,
     FCC + 0.02 jitter, TVN."""
-    rng = np.random.default_rng(seed)
-    return [ljgb.config(n=int(rng.integers(200, 4000)), density=float(rng.uniform(0.01, 1.1)),
-                        temperature=float(rng.uniform(0.7, 2.0)), canonical=1, boundary=i % 2,
-                        lattice=ljgb.LATTICE_FCC, jitter=0.02, seed=1000 + i) for i in range(k)]
+    return ljgb.replica_batch_configs(seed, k)
 
 
 def extra_configs(torch, ljgb, oracle, dev, flush, peak):

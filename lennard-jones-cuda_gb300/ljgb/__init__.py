@@ -217,6 +217,17 @@ def pinned(shape, dtype=np.float64) -> np.ndarray:
     return arr
 
 
+def replica_batch_configs(seed: int = 3, k: int = 256):
+    """The batched-replicas workload: k boxes with N uniform in [200, 4000),
+    rho* in [0.01, 1.1], T* in [0.7, 2.0], periodic and hard-wall boxes
+    alternating, FCC + 0.02 sigma jitter, TVN (seeded)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [config(n=int(rng.integers(200, 4000)), density=float(rng.uniform(0.01, 1.1)),
+                   temperature=float(rng.uniform(0.7, 2.0)), canonical=1, boundary=i % 2,
+                   lattice=LATTICE_FCC, jitter=0.02, seed=1000 + i) for i in range(k)]
+
+
 def reference_rdf_dr2(n: int) -> float:
     return float(load().lj_reference_rdf_dr2(int(n)))
 

@@ -40,7 +40,31 @@ def main(argv=None):
                          "dropped, 2: linear r bins to L/2)")
     ap.add_argument("--velo", action="store_true", help="after the steps, time --calls speed histograms")
     ap.add_argument("--calls", type=int, default=20)
+    ap.add_argument("--batch", type=int, default=0, metavar="K",
+                    help="run the batched-replicas workload instead: K boxes (N in [200, 4000), rho* in [0.01, 1.1], "
+                         "T* in [0.7, 2.0], half hard-wall, TVN, dt 0.004); --shape as above")
     a = ap.parse_args(argv)
+    if a.batch > 0:
+        cfgs = ljgb.replica_batch_configs(3, a.batch)
+        b = ljgb.System(batch=cfgs)
+        if a.shape >= 0:
+            b.set_kernel_shape(a.shape)
+        else:
+            b.autotune()
+        b.integrate(0.004, 2)
+        b.profile(True)
+        b.integrate(0.004, a.steps)
+        p = b.profile_read()
+        b.profile(False)
+        obs = b.batch_observables()
+        pairs = float(sum(c.n * (c.n - 1) for c in cfgs))
+        step_ms = p["step_ms"] / max(1, p["steps"])
+        print("batch of %d boxes (sum N %d): pair kernel %.4f ms, step %.4f ms, %.3e pair-interactions/s, "
+              "U/N of box 0 %.6f, tune %s" % (a.batch, sum(c.n for c in cfgs), p["pair_ms"] / max(1, p["pair_launches"]),
+                                              step_ms, pairs / (step_ms * 1e-3), obs[0]["U"] / cfgs[0].n,
+                                              {k: v for k, v in b.tune_info().items() if k != "shapes"}))
+        b.close()
+        return
     if a.adjoint > 0:
         adj = ljgb.Adjoint(n=a.n, density=a.rho, temperature=a.T, lattice=ljgb.LATTICE_FCC if a.fcc else
                            ljgb.LATTICE_SC, jitter=a.jitter, seed=a.seed, checkpoint_every=a.adjoint)
