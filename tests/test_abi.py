@@ -172,6 +172,20 @@ def test_schedule_covers_every_pair_once(ljlib, n, block, tile, ctas):
     assert cost.max() <= cost.mean() + 2 * (grain + 8)
 
 
+@pytest.mark.parametrize("n", [200, 1500, 3001, 7777, 16384])
+@pytest.mark.parametrize("cap", [1, 2, 3, 8, 32])
+def test_split_cap_bounds_threads_per_particle(ljlib, n, cap):
+    """A handle with split cap k runs min(SMs x resident CTAs, k x i-blocks)
+    CTAs.  Every i-block of one box costs the same (all j), so the equal-cost
+    cuts give no block more than k segments: at most k threads per particle."""
+    import ljgb
+    nbt = (n + 127) // 128
+    for tile in (256, 512):
+        s = ljgb.schedule_plan([n], 128, tile, min(912, nbt * cap))
+        seg = s["blocks"][:, 6]
+        assert seg.max() <= cap and seg.min() >= 1
+
+
 def test_schedule_rejects_bad_input(ljlib):
     import ljgb
     with pytest.raises(ljgb.LJError):
