@@ -550,8 +550,13 @@ lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
   lj_status st = fused ? enqueue_step_fused(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels)
                        : enqueue_step(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels);
   cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
-  if (st) return st;
-  LJ_CUDA(s, ce);
+  if (st || ce != cudaSuccess) {  // nothing of a failed capture is kept
+    if (g) cudaGraphDestroy(g);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (st) return st;
+    LJ_CUDA(s, ce);
+  }
   if (ge.profiled) {
     size_t nn = 0;
     LJ_CUDA(s, cudaGraphGetNodes(g, nullptr, &nn));
