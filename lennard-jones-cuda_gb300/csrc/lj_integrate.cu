@@ -534,13 +534,6 @@ __global__ void k_unpack(const double* __restrict__ in, double* __restrict__ out
   for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
 }
 
-__global__ void k_pack(const double* __restrict__ in, double* __restrict__ out, int n, int npad) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) out[3 * (size_t)i + c] = in[(size_t)c * npad + i];
-}
-
 // Up to three (N,3) <-> component-major transposes in one launch; blockIdx.y
 // selects the array.
 __global__ void k_pack_multi(XyzArrays a, int n, int npad) {
@@ -615,11 +608,6 @@ cudaError_t launch_unpack_multi_checked(const XyzArrays& a, int count, int n, in
                                         cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
   k_unpack_multi_checked<<<dim3((n + 255) / 256, count), 256, 0, st>>>(a, n, npad, bad);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st) {
-  k_pack<<<(n + 255) / 256, 256, 0, st>>>(in, out, n, npad);
   return cudaGetLastError();
 }
 

@@ -138,7 +138,6 @@ struct CounterDev {
 cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* row, int n,
                             cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
-cudaError_t launch_pack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_selftest_wait(int* status, cudaStream_t st);
 cudaError_t launch_check_finite(const double* in, size_t count, int* bad, cudaStream_t st);
 // Up to three (N,3) interleaved <-> component-major [3][npad] transposes in one launch.
