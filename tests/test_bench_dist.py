@@ -56,3 +56,28 @@ def test_reference_arm_runs_on_rank_zero_only():
     class A:
         steps, warmup = 1, 1
     assert bench.reference_arm(A(), rank=1, world=2) is None
+
+
+def test_clock_samples_kept_only_inside_the_timed_region():
+    """bench.ClockSampler summarises the nvidia-smi lines stamped between the
+    start and the end of the timed region (plus one sampling interval): the
+    median SM clock, the maximum, and any throttle reason seen active."""
+    import sys
+    sys.path.insert(0, REPO)
+    import bench
+    c = bench.ClockSampler(0)
+    c.t_begin, c.t_end = 10.0, 11.0
+    line = "0, {sm}, 2070, 900.5, 0x0, {hw}, Not Active, Not Active, {pc}"
+    c.lines = [
+        (9.5, line.format(sm=800, hw="Active", pc="Not Active")),       # before: ignored
+        (10.1, line.format(sm=2070, hw="Not Active", pc="Not Active")),
+        (10.5, line.format(sm=2055, hw="Not Active", pc="Active")),
+        (11.01, line.format(sm=2070, hw="Not Active", pc="Not Active")),  # within one interval after
+        (11.5, line.format(sm=700, hw="Active", pc="Not Active")),      # after: ignored
+        (10.7, "garbage"),
+    ]
+    s = c.summary()
+    assert s["samples"] == 3
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    assert s["region_s"] == pytest.approx(1.0)
