@@ -41,9 +41,22 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref() -> bool:
-    """Build oracle/_ref from the reference sources when they are present."""
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
+def reference_dir(ref_dir: str = None):
+    """The vlvovch/lennard-jones-cuda checkout to build oracle/_ref from:
+    ref_dir, else LJ_REFERENCE_DIR; None unless it holds the reference's
+    src/library/MDSystem.cpp."""
+    d = ref_dir or os.environ.get("LJ_REFERENCE_DIR")
+    if d and os.path.isfile(os.path.join(d, "src", "library", "MDSystem.cpp")):
+        return d
+    return None
+
+
+def build_ref(ref_dir: str = None) -> bool:
+    """Build oracle/_ref from the reference sources when they are present
+    (see reference_dir); True if the reference library exists afterwards."""
+    d = reference_dir(ref_dir)
+    if d is not None:
+        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), d])
     return os.path.exists(REF_PATH)
 
 

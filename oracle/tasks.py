@@ -20,6 +20,12 @@ never imports, links or calls it).
   * gce_nsub: GetNsub of src/tasks/semiGCEfluctuations/
     semiGCEfluctuations.cpp:7-25 (particles in the cube of volume fraction f
     around the box centre).
+
+Parity is pinned: tests/golden/stats_reference.npz holds the reference's own
+TimeAverage / NumberStatistics outputs on seeded series (compiled from its
+headers by oracle/build_ref.sh into oracle/_ref/ref_stats and run by
+tests/golden/make_stats_golden.py); tests/test_tasks.py checks these
+functions and include/ljgb/Statistics.hpp against them.
 """
 from __future__ import annotations
 

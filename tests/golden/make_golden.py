@@ -7,8 +7,9 @@ forces, observables, RDF counts, velocity histograms and trajectories.
 The reference has no tests or golden vectors of its own, so these fixtures
 are what pins the oracle restatement (oracle/lj_oracle.c) to the reference.
 
-Usage (needs the reference sources; not run by the test suite):
-    python tests/golden/make_golden.py
+Usage (needs the reference sources, given as LJ_REFERENCE_DIR or the first
+argument; not run by the test suite):
+    python tests/golden/make_golden.py <reference checkout>
 """
 from __future__ import annotations
 
@@ -96,7 +97,7 @@ def make_case(name, N, rho, T0, canonical, bc, lattice, jitter, seed, dt, steps,
 
 
 def main():
-    if not O.ref_available() and not O.build_ref():
+    if not O.ref_available() and not O.build_ref(sys.argv[1] if len(sys.argv) > 1 else None):
         raise SystemExit("reference sources unavailable; cannot regenerate golden fixtures")
     for case in CASES:
         make_case(*case)

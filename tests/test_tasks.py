@@ -13,11 +13,17 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INC = os.path.join(REPO, "include")
 
 
+_BUILT = {}
+
+
 def _compile(tmp_path, name):
-    exe = str(tmp_path / name)
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", INC, os.path.join(REPO, "tests", "tasks", name + ".cpp"),
-                           "-o", exe])
-    return exe
+    """g++ build of tests/tasks/<name>.cpp, once per test session."""
+    if name not in _BUILT:
+        exe = str(tmp_path / name)
+        subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", INC,
+                               os.path.join(REPO, "tests", "tasks", name + ".cpp"), "-o", exe])
+        _BUILT[name] = exe
+    return _BUILT[name]
 
 
 def _parse(line):
@@ -55,6 +61,57 @@ def test_statistics_match_reference_formulas(tmp_path, kind):
     assert got["ta_err"] == pytest.approx(ref["mean_err"] * np.sqrt(s), rel=1e-6)
     if kind == "ar1":  # s ~ 2/(-ln 0.9) ~ 19 for an AR(1) with coefficient 0.9
         assert 12 < s < 28
+
+
+STATS_GOLDEN = os.path.join(REPO, "tests", "golden", "stats_reference.npz")
+STATS_SERIES = ("counts_binomial", "counts_correlated", "ar1_pressure", "energy_shifted", "gamma_skewed",
+                "anticorrelated", "short")
+
+
+@pytest.mark.parametrize("name", STATS_SERIES)
+def test_statistics_pinned_to_reference(tmp_path, name):
+    """The numpy restatement (oracle/tasks.py) and Statistics.hpp against the
+    reference's own TimeAverage / NumberStatistics run on the same series
+    (fixtures written by tests/golden/make_stats_golden.py)."""
+    import tasks
+    z = np.load(STATS_GOLDEN)
+    fields = [str(f) for f in z["fields"]]
+    x = z[name + "__x"]
+    ref = dict(zip(fields, z[name + "__ref"]))              # as the task drivers call it
+    first = dict(zip(fields, z[name + "__ref_first"]))      # power sums about x[0]
+    assert ref["n"] == len(x)
+    # mean, variance, error of the mean, scaled variance and its error
+    m = tasks.moments(x)
+    for k in ("mean", "var", "mean_err", "w", "w_err"):
+        assert m[k] == pytest.approx(ref[k], rel=1e-9), k
+    # cumulant ratios: the restatement's moment sums about a given shift
+    # reproduce the reference's with the same shift
+    with np.errstate(invalid="ignore", divide="ignore"):   # the constant-free short series
+        cr = tasks.cumulant_ratios(x, shift=x[0])
+    for k in ("skew", "skew_err", "kurt", "kurt_err"):
+        if np.isfinite(first[k]):
+            assert cr[k] == pytest.approx(first[k], rel=1e-10, abs=1e-15), k
+    # statistical inefficiency: the reference's where it is finite; 1 where
+    # its logarithm's argument is negative (NaN there, a stated difference)
+    s = tasks.inefficiency(x)
+    if np.isfinite(ref["s"]):
+        assert s == pytest.approx(ref["s"], rel=1e-9)
+        assert m["mean_err"] * np.sqrt(s) == pytest.approx(ref["ta_err"], rel=1e-9)
+    else:
+        assert s == 1.0
+    # include/ljgb/Statistics.hpp (moments summed about the first observation)
+    exe = _compile(tmp_path, "stats_check")
+    out = subprocess.run([exe], input="\n".join("%.17g" % v for v in x), capture_output=True, text=True, check=True)
+    got = {k: float(v) for k, v in _parse(out.stdout).items()}
+    assert got["n"] == len(x)
+    for k in ("mean", "var", "mean_err", "w", "w_err", "skew", "skew_err", "kurt", "kurt_err"):
+        if np.isfinite(first[k]):
+            assert got[k] == pytest.approx(first[k], rel=1e-9, abs=1e-15), k
+    if np.isfinite(ref["s"]):
+        assert got["s"] == pytest.approx(ref["s"], rel=1e-9)
+        assert got["ta_err"] == pytest.approx(ref["ta_err"], rel=1e-9)
+    else:
+        assert got["s"] == 1.0
 
 
 def test_parameter_file_format(tmp_path):
