@@ -259,6 +259,9 @@ int64_t lj_kernel_launch_count(const lj_system* sys);
 lj_status lj_batch_create(const lj_config* cfgs, int32_t nsys, lj_system** out);
 /* Observables of every box (nsys entries), synchronising. */
 lj_status lj_batch_observables(lj_system* sys, lj_observables* out);
+/* Per-step records of box `box` of a batch (lj_set_recording keeps cap steps
+ * of every box), oldest first, like lj_get_records (which reads box 0). */
+lj_status lj_batch_records(lj_system* sys, int32_t box, lj_observables* out, int32_t max, int32_t* count);
 /* Number of boxes and the particle offset of each (offsets: nsys + 1 entries). */
 lj_status lj_batch_info(const lj_system* sys, int32_t* nsys, int32_t* offsets);
 

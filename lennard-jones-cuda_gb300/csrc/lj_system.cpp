@@ -1149,8 +1149,10 @@ lj_status lj_set_recording(lj_system* s, int32_t cap) {
   return write_scalars(s, sc);
 }
 
-lj_status lj_get_records(lj_system* s, lj_observables* out, int32_t max, int32_t* count) {
-  if (!s || !count || max < 0) return LJ_ERR_INVALID;
+// Copies box `box`'s ring of per-step records (rec_cap entries at
+// records + box * rec_cap, written by the step epilogues), oldest first.
+static lj_status read_records(lj_system* s, int box, lj_observables* out, int32_t max, int32_t* count) {
+  if (!s || !count || max < 0 || box < 0 || box >= s->nsys) return LJ_ERR_INVALID;
   DeviceGuard device_guard(s->device);
   lj_status st = check_status(s);
   if (st) return st;
@@ -1159,8 +1161,9 @@ lj_status lj_get_records(lj_system* s, lj_observables* out, int32_t max, int32_t
   std::vector<DevScalars> sc;
   if ((st = read_scalars(s, sc))) return st;
   std::vector<DevRecord> rec(s->rec_cap);
-  LJ_CUDA(s, cudaMemcpy(rec.data(), s->records.p, sizeof(DevRecord) * s->rec_cap, cudaMemcpyDeviceToHost));
-  const long long total = sc[0].rec_count;
+  LJ_CUDA(s, cudaMemcpy(rec.data(), s->records.p + (size_t)box * s->rec_cap, sizeof(DevRecord) * s->rec_cap,
+                        cudaMemcpyDeviceToHost));
+  const long long total = sc[box].rec_count;
   const long long have = std::min<long long>(total, s->rec_cap);
   const long long first = total - have;
   int n = 0;
@@ -1184,6 +1187,14 @@ lj_status lj_get_records(lj_system* s, lj_observables* out, int32_t max, int32_t
   }
   *count = n;
   return LJ_OK;
+}
+
+lj_status lj_get_records(lj_system* s, lj_observables* out, int32_t max, int32_t* count) {
+  return read_records(s, 0, out, max, count);
+}
+
+lj_status lj_batch_records(lj_system* s, int32_t box, lj_observables* out, int32_t max, int32_t* count) {
+  return read_records(s, box, out, max, count);
 }
 
 lj_status lj_reset_averaging(lj_system* s) {

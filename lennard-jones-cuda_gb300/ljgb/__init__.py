@@ -88,6 +88,7 @@ def _declare(L):
         "lj_batch_info": (C.c_int, [_P, C.POINTER(C.c_int32), _P]),
         "lj_set_recording": (C.c_int, [_P, C.c_int32]),
         "lj_get_records": (C.c_int, [_P, C.POINTER(Observables), C.c_int32, C.POINTER(C.c_int32)]),
+        "lj_batch_records": (C.c_int, [_P, C.c_int32, C.POINTER(Observables), C.c_int32, C.POINTER(C.c_int32)]),
         "lj_reset_averaging": (C.c_int, [_P]),
         "lj_set_canonical": (C.c_int, [_P, C.c_int32]),
         "lj_set_boundary": (C.c_int, [_P, C.c_int32]),
@@ -377,6 +378,12 @@ class System:
         arr = (Observables * max_records)()
         cnt = C.c_int32()
         self._c(load().lj_get_records(self.h, arr, max_records, C.byref(cnt)))
+        return [arr[k].as_dict() for k in range(cnt.value)]
+
+    def batch_records(self, box: int, max_records: int = 1 << 20):
+        arr = (Observables * max_records)()
+        cnt = C.c_int32()
+        self._c(load().lj_batch_records(self.h, int(box), arr, max_records, C.byref(cnt)))
         return [arr[k].as_dict() for k in range(cnt.value)]
 
     def reset_averaging(self):

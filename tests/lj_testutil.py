@@ -40,3 +40,12 @@ def force_errors(F, Fref):
     return dict(rel_median=float(np.median(rel)), rel_p99=float(np.percentile(rel, 99)),
                 rel_max=float(rel.max()), rms_max=float(relrms.max()), rms_median=float(np.median(relrms)),
                 gate_max=float(mixed.max()))
+
+
+def golden_states():
+    """The golden MDSystem state fixtures (tests/golden/n*.npz, written by the
+    reference's CPU MDSystem); tests/golden/stats_*.npz pin the statistics."""
+    import glob
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    return sorted(p for p in glob.glob(os.path.join(here, "*.npz")) if not os.path.basename(p).startswith("stats_"))

@@ -7,9 +7,11 @@ and checks it against the FP64 oracle or the all-FP64 GPU path:
   * plain method: N=400, rho*=0.05, T*=1.4, SC lattice +-0.05 sigma jitter,
     Maxwell velocities, dt=0.005, EVN, 1000 steps, FP64; per-step K, V, W
     against the FP64 oracle and a 200-bin RDF to r = L/2;
-  * dense liquid: N=16384, rho*=0.85, T*=1.0, FCC +-0.02, dt=0.005, TVN;
-    mixed precision step by step (first 10 steps) against the all-FP64 run,
-    then time averages of U/N and P against the all-FP64 run;
+  * dense liquid: N=16384, rho*=0.85, T*=1.0, FCC +-0.02, dt=0.005, TVN,
+    10^4 steps; mixed precision step by step (first 10 steps) against the
+    all-FP64 run, then time averages of U/N, P and g(r) against it;
+  * batched replicas: 256 boxes, 5000 TVN steps; per-replica averages of a
+    sample against all-FP64 runs;
   * large single system: N=262144, rho*=1.1 (solid), T*=1.0, FCC +-0.01,
     dt=0.004, TVN; forces on a 4096-particle seeded subset against the FP64
     oracle, then TVN steps;
@@ -21,13 +23,6 @@ import pytest
 import lj_testutil as U
 
 pytestmark = pytest.mark.gpu
-
-
-def _blocks_sem(x, nblocks=10):
-    """Standard error of the mean from block averages."""
-    b = np.array_split(np.asarray(x), nblocks)
-    m = np.array([blk.mean() for blk in b])
-    return m.std(ddof=1) / np.sqrt(len(m))
 
 
 def test_plain_method_configuration(ljgb_mod, oracle_mod):
@@ -67,8 +62,22 @@ def test_plain_method_configuration(ljgb_mod, oracle_mod):
     assert abs(int(got.sum()) - int((r < s.L / 2).sum())) <= 4
 
 
+def time_average(x):
+    """Mean and its error the way the reference's TimeAverage forms them
+    (src/tasks/auxiliary/time-average-aux.h:27-67): the error of the mean
+    scaled by the square root of the statistical inefficiency."""
+    import tasks
+    m = tasks.moments(x)
+    return m["mean"], m["mean_err"] * np.sqrt(tasks.inefficiency(x))
+
+
 def test_dense_liquid_configuration(ljgb_mod):
+    """N=16384, rho*=0.85, T*=1.0, FCC +-0.02, dt=0.005, TVN for 10^4 steps,
+    mixed precision against the all-FP64 run: step by step for the first 10
+    steps, then time averages of U/N, P and g(r) over steps 1001..10000
+    within their statistical errors."""
     N, rho, T0, dt = 16384, 0.85, 1.0, 0.005
+    S, S_eq, blk = 10000, 1000, 100
     kw = dict(n=N, density=rho, temperature=T0, canonical=1, lattice=ljgb_mod.LATTICE_FCC, jitter=0.02, seed=2)
     mixed = ljgb_mod.System(**kw, precision=ljgb_mod.PREC_MIXED)
     fp64 = ljgb_mod.System(**kw, precision=ljgb_mod.PREC_FP64)
@@ -92,45 +101,109 @@ def test_dense_liquid_configuration(ljgb_mod):
         assert om["T"] == pytest.approx(od["T"], rel=1e-7)
         assert om["U"] == pytest.approx(od["U"], rel=1e-6)
         assert om["P"] == pytest.approx(od["P"], rel=1e-5)
-    # averages: both runs continue; trajectories decorrelate, the averages
-    # must agree within their statistical errors (U/N, P and g(r), the last
-    # summed on the device after every step, 100 linear bins to L/2, read in
-    # blocks of 50 steps for its error)
-    n_avg, nblk, nbr = 400, 8, 100
+    # Both runs continue to step S.  The trajectories decorrelate; the
+    # averages after equilibration must agree within their statistical
+    # errors: U/N and P from the per-step records, g(r) summed on the device
+    # after every step (100 linear bins to L/2) and read every 100 steps.
+    nbr = 100
     width = (L / 2) / nbr
     # ordered pairs per step of an ideal gas in each shell: N rho 4/3 pi (r1^3 - r0^3)
     edges = width * np.arange(nbr + 1)
     ideal = N * rho * 4.0 / 3.0 * np.pi * (edges[1:] ** 3 - edges[:-1] ** 3)
-    g = {}
+    g, series = {}, {}
     for name, s in (("mixed", mixed), ("fp64", fp64)):
-        s.set_recording(n_avg)
+        s.set_recording(S - S_eq)
         s.rdf_accumulate(True, mode=ljgb_mod.RDF_R_LINEAR, nbins=nbr, width=width)
-        blocks = []
-        for _ in range(nblk):
-            s.integrate(dt, n_avg // nblk)
+        done, blocks = 10, []
+        while done < S:
+            k = blk - done % blk
+            s.integrate(dt, k)
             c, ns = s.rdf_accumulated(reset=True)
-            assert ns == n_avg // nblk
-            blocks.append(c.astype(np.float64) / ns / ideal)
-        g[name] = np.array(blocks)
+            assert ns == k
+            done += k
+            if done > S_eq:
+                blocks.append(c.astype(np.float64) / ns / ideal)
         s.rdf_accumulate(False)
-    gm, gd = g["mixed"].mean(0), g["fp64"].mean(0)
-    sem = np.hypot(g["mixed"].std(0, ddof=1), g["fp64"].std(0, ddof=1)) / np.sqrt(nblk)
-    dev = np.abs(gm - gd) / (sem + 2e-3 * gd.max())
-    print("dense liquid g(r) over %d steps: first peak g=%.4f at r=%.3f, max |mixed - fp64| / error %.2f "
-          "(max |dg| %.2e)" % (n_avg, gd.max(), (gd.argmax() + 0.5) * width, dev.max(), np.abs(gm - gd).max()))
-    assert 2.0 < gd.max() < 4.0 and abs(gd[-10:].mean() - 1.0) < 0.05
-    assert dev.max() < 6
-    res = {}
-    for name, s in (("mixed", mixed), ("fp64", fp64)):
-        rec = s.records()
-        u = np.array([r["U"] for r in rec]) / N
-        p = np.array([r["P"] for r in rec])
-        res[name] = (u.mean(), _blocks_sem(u), p.mean(), _blocks_sem(p))
-    (um, su_m, pm_, sp_m), (ud, su_d, pd_, sp_d) = res["mixed"], res["fp64"]
-    print("dense liquid averages over %d steps: U/N %.8f (mixed) %.8f (fp64) +-%.1e; P %.7f / %.7f +-%.1e"
-          % (n_avg, um, ud, su_d, pm_, pd_, sp_d))
-    assert abs(um - ud) < 5 * np.hypot(su_m, su_d) + 1e-4
-    assert abs(pm_ - pd_) < 5 * np.hypot(sp_m, sp_d) + 1e-3
+        g[name] = np.array(blocks)
+        rec = s.records(max_records=S - S_eq)
+        assert len(rec) == S - S_eq and rec[0]["step"] == S_eq + 1 and rec[-1]["step"] == S
+        series[name] = (np.array([r["U"] for r in rec]) / N, np.array([r["P"] for r in rec]),
+                        np.array([r["T"] for r in rec]))
+    assert len(g["mixed"]) == (S - S_eq) // blk
+    # g(r): per-bin time averages of the 100-step block means
+    gm = np.array([time_average(col) for col in g["mixed"].T])
+    gd = np.array([time_average(col) for col in g["fp64"].T])
+    err_g = np.hypot(gm[:, 1], gd[:, 1])
+    dev_g = np.abs(gm[:, 0] - gd[:, 0]) / (err_g + 1e-3 * gd[:, 0].max())
+    print("dense liquid g(r) over steps %d..%d: first peak g=%.4f at r=%.3f, max |mixed - fp64| / error %.2f "
+          "(max |dg| %.2e)" % (S_eq + 1, S, gd[:, 0].max(), (gd[:, 0].argmax() + 0.5) * width, dev_g.max(),
+                               np.abs(gm[:, 0] - gd[:, 0]).max()))
+    assert 2.0 < gd[:, 0].max() < 4.0 and abs(gd[-10:, 0].mean() - 1.0) < 0.05
+    assert dev_g.max() < 5
+    for q, label, floor in ((0, "U/N", 1e-4), (1, "P", 1e-3)):
+        am, em = time_average(series["mixed"][q])
+        ad, ed = time_average(series["fp64"][q])
+        print("dense liquid <%s> over steps %d..%d: %.7f +- %.1e (mixed), %.7f +- %.1e (fp64), "
+              "difference %.2f sigma" % (label, S_eq + 1, S, am, em, ad, ed, abs(am - ad) / np.hypot(em, ed)))
+        assert abs(am - ad) < 4 * np.hypot(em, ed) + floor, label
+    # TVN holds the kinetic temperature of both runs at T0
+    for name in ("mixed", "fp64"):
+        assert abs(series[name][2].mean() - T0) < 5e-3, name
+
+
+def test_batched_replicas_configuration(ljgb_mod):
+    """256 replicas (N uniform in [200, 4000), rho* in [0.01, 1.1], T* in
+    [0.7, 2.0], periodic and hard-wall boxes alternating), dt=0.004, 5000 TVN
+    steps in one launch per step, autotuned and graph-captured.  Every
+    replica stays finite, in its box and at its temperature; the per-replica
+    time averages of U/N and P over steps 1001..5000 of a seeded sample of 8
+    replicas (4 periodic, 4 walled) agree with all-FP64 runs of the same
+    replicas within their statistical errors."""
+    S, S_eq, dt = 5000, 1000, 0.004
+    cfgs = ljgb_mod.replica_batch_configs(seed=3, k=256)
+    b = ljgb_mod.System(batch=cfgs)
+    b.autotune()
+    b.set_recording(S - S_eq)
+    b.integrate(dt, S)
+    obs = b.batch_observables()
+    p, _, _ = b.get_state()
+    for k, (c, o) in enumerate(zip(cfgs, obs)):
+        assert o["step"] == S and np.isfinite(o["U"]) and np.isfinite(o["P"]), k
+        L = (c.n / c.density) ** (1 / 3)
+        pk = p[b.offsets[k]:b.offsets[k + 1]]
+        if c.boundary == 1:
+            assert pk.min() > -0.5 and pk.max() < L + 0.5, k
+        # TVN holds the kinetic temperature at T0 in every replica
+        Tk = np.array([r["T"] for r in b.batch_records(k, max_records=S - S_eq)])
+        assert len(Tk) == S - S_eq and abs(Tk.mean() - c.temperature) < 0.03 * c.temperature, k
+    rng = np.random.default_rng(8)
+    sample = sorted(list(rng.choice(np.arange(0, 256, 2), 4, replace=False)) +
+                    list(rng.choice(np.arange(1, 256, 2), 4, replace=False)))
+    ref_cfgs = ljgb_mod.replica_batch_configs(seed=3, k=256)
+    sel = [ref_cfgs[k] for k in sample]
+    for c in sel:
+        c.precision = ljgb_mod.PREC_FP64
+    d = ljgb_mod.System(batch=sel)
+    d.set_recording(S - S_eq)
+    d.integrate(dt, S)
+    worst = 0.0
+    for j, k in enumerate(sample):
+        c = cfgs[k]
+        rm = b.batch_records(k, max_records=S - S_eq)
+        rd = d.batch_records(j, max_records=S - S_eq)
+        assert len(rm) == len(rd) == S - S_eq and rm[-1]["step"] == rd[-1]["step"] == S
+        line = []
+        for key, scale, floor in (("U", 1.0 / c.n, 1e-4), ("P", 1.0, 1e-4)):
+            am, em = time_average(np.array([r[key] for r in rm]) * scale)
+            ad, ed = time_average(np.array([r[key] for r in rd]) * scale)
+            dev = abs(am - ad) / (np.hypot(em, ed) + floor)
+            worst = max(worst, dev)
+            line.append("<%s> %.6f +- %.1e / %.6f +- %.1e (%.2f sigma)" % (
+                "U/N" if key == "U" else "P", am, em, ad, ed, dev))
+            assert abs(am - ad) < 5 * np.hypot(em, ed) + floor, (k, key)
+        print("replica %3d (N=%d rho*=%.3f T*=%.3f %s): %s" % (k, c.n, c.density, c.temperature,
+                                                             "wall" if c.boundary else "periodic", "; ".join(line)))
+    print("batched replicas: largest mixed-vs-FP64 deviation %.2f sigma" % worst)
 
 
 def test_large_single_system_configuration(ljgb_mod, oracle_mod):

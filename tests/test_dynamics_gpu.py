@@ -5,7 +5,6 @@ temperature Verlet (TVN) with the FP64 oracle restatement of
 MDSystem::Integrate (MDSystem.cpp:438-583), on identical seeded states,
 through the C ABI.
 """
-import glob
 import os
 
 import numpy as np
@@ -15,7 +14,7 @@ import lj_testutil as U
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = U.golden_states()
 
 
 def run_pair(ljgb, oracle_mod, pos, vel, N, rho, T0, canonical, bc, dt, steps, prec):
@@ -220,7 +219,6 @@ def test_fused_matches_unfused_path(ljgb_mod, boundary):
     the fused mixed path with the FP64 path over 30 steps of both ensembles.
     With walls, one particle starts outside the box moving away from it: the
     frame takes in the starting positions, and the wall turns it back."""
-    import lj_testutil as U
     N, rho = 3000, 0.8
     pos, vel, L = U.lattice_state(N, rho, 1.1, "fcc", 0.02, seed=21)
     if boundary == 1:

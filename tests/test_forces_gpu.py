@@ -10,7 +10,6 @@ V within 2e-6 and the virial W within 1e-5 relative (W = sum 4(12A - 6B)
 cancels the r^-12 and r^-6 sums by ~15x in a liquid).  The FP64 path must
 agree to 1e-11.
 """
-import glob
 import os
 
 import numpy as np
@@ -20,7 +19,7 @@ import lj_testutil as U
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = U.golden_states()
 MIXED_GATE_TOL = 1e-5
 MIXED_MEDIAN_TOL = 1e-5
 ENERGY_TOL = 2e-6

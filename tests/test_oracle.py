@@ -6,13 +6,14 @@ The golden fixtures were produced by the reference's own MDSystem.cpp
 agree within the reference's float-storage error; analytic known answers pin
 the physics independently of both.
 """
-import glob
 import os
 
 import numpy as np
 import pytest
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+import lj_testutil as U
+
+GOLDEN = U.golden_states()
 SCALARS = ("U", "T", "K", "V", "P", "Pshear", "t", "L", "av_U", "av_T", "av_p", "av_iters", "rdf_dr2")
 
 

@@ -2,15 +2,16 @@
 this library (GPU tests): the call sequence MDSystem::CalculateForces makes
 in GPU mode (MDSystem.cpp:240-251), on the golden states."""
 import ctypes as C
-import glob
 import os
 
 import numpy as np
 import pytest
 
+import lj_testutil as U
+
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = U.golden_states()
 
 
 def calculate_n_forces(L, pos4, box, periodic, dr2, block=256):

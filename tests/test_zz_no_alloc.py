@@ -8,15 +8,16 @@ in a fresh process and after the other tests (which leave the array holding
 another call's contents, or none).
 """
 import ctypes as C
-import glob
 import os
 
 import numpy as np
 import pytest
 
+import lj_testutil as U
+
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = U.golden_states()
 
 
 def bind(lib):
@@ -87,7 +88,6 @@ def test_static_matches_existing_entry_point_twice(ljlib):
 
 
 def test_static_dense_box_two_calls(ljlib):
-    import lj_testutil as U
     fn = bind(ljlib)
     n = 4000
     pos, _, L = U.lattice_state(n, 0.85, 1.0, "fcc", 0.02, seed=11)
