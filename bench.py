@@ -57,6 +57,13 @@ FLOPS_PER_PAIR = 38  # algorithmic FP32 flops per ordered pair, FMA = 2, rcp = 1
 WORKLOAD = "lj-dense-liquid-tvn N=16384 rho*=0.85 T*=1.0 FCC+0.02 dt=0.005"
 
 
+def bench_config(world: int) -> dict:
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": WORKLOAD, "n": N, "rho": RHO, "T": T0, "dt": DT, "ensemble": "TVN",
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "GPU arm: flushed (256 MB write) before every timed step"}
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -132,11 +139,11 @@ class ClockSampler:
 # CPU arm: the reference's CPU algorithm (faithful float-storage restatement)
 # ---------------------------------------------------------------------------
 def cpu_state():
-    import ljgb
-    cfg = ljgb.config(n=N, temperature=T0, density=RHO, canonical=1, lattice=ljgb.LATTICE_FCC, jitter=JITTER,
-                      seed=SEED)
-    pos, vel = ljgb.sample_initial_state(cfg)
-    L = (N / RHO) ** (1.0 / 3.0)
+    """The workload's seeded initial state as float4 arrays, drawn by the
+    oracle's restatement of the library's sampler (the same numbers; the CPU
+    arm never loads the product library)."""
+    import oracle
+    pos, vel, L = oracle.sample_state(N, RHO, T0, lattice=1, jitter=JITTER, seed=SEED)
     p4 = np.zeros((N, 4), np.float32)
     p4[:, :3] = pos
     p4[:, 3] = np.float32(L / 150.0)
@@ -481,10 +488,8 @@ def gpu_arm(args, rank, world, local_rank):
             "metric": "pair-interactions/s, N=16384, FP32-mixed vs FP64 same GB300 @ force rel err<=1e-5",
             "value": value, "unit": "pair-interactions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32-pairs/f64-state", "data": "synthetic (seeded FCC+jitter, Maxwell)",
-            "config": {"workload": WORKLOAD, "n": N, "rho": RHO, "T": T0, "dt": DT, "ensemble": "TVN",
-                       "parallelism": "replicas" if world > 1 else "single", "l2": "flushed (256 MB write) "
-                       "before every timed step", "kernel_shape": shape},
+            "vs_baseline": None, "dtype": "f32-pairs/f64-state", "data": "synthetic (seeded FCC+jitter)",
+            "config": bench_config(world), "kernel_shape": shape,
             "steps_per_s": 1e3 / ms_step,
             "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step":
                     e2e_bytes["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e_bytes["d2h_bytes_per_step"],
@@ -512,36 +517,49 @@ def gpu_arm(args, rank, world, local_rank):
 def reference_arm(args, rank, world):
     if rank != 0:
         return None
-    # Each "step" is one full N=16384 TVN step of the reference CPU algorithm;
-    # the run is capped so that warm-up + steps stay within a few minutes.
+    # Each step is a bounded sample of one N=16384 step of the reference CPU
+    # algorithm: its force loop (MDSystem.cpp:237-311, restated bit-exactly)
+    # over a slice of the rows, rotating through all N rows, sized so that
+    # warm-up + steps stay within about 150 s.  The O(N) integration of a
+    # step is left out of the sample (well under 0.1% of a step at this N).
     import oracle
     oracle.build()
     threads = oracle.default_threads()
     p4, v4 = cpu_state()
     r = oracle.R32System(N, T0, RHO, True, 0, p4, v4)
-    r.calculate_forces(threads)
-    r.calculate_parameters()
     t0 = time.perf_counter()
-    r.integrate(DT, threads)
-    one = time.perf_counter() - t0
+    r.calculate_forces(threads)                      # calibration: one full force evaluation
+    full = time.perf_counter() - t0
     budget = 150.0
-    steps = max(1, min(args.steps, int(budget / max(one, 1e-3)) - 1))
-    for _ in range(max(0, min(args.warmup, 1) - 1)):
-        r.integrate(DT, threads)
+    rows = max(64, min(N, int(N * budget / max(args.steps + args.warmup, 1) / max(full, 1e-6))))
+    cursor = [0]
+
+    def step():
+        i0 = cursor[0]
+        i1 = min(N, i0 + rows)
+        r.force_rows(i0, i1, threads)
+        cursor[0] = 0 if i1 >= N else i1
+        return (i1 - i0) * (N - 1)
+
+    for _ in range(args.warmup):
+        step()
+    pairs = 0
     t0 = time.perf_counter()
-    for _ in range(steps):
-        r.integrate(DT, threads)
+    for _ in range(args.steps):
+        pairs += step()
     el = time.perf_counter() - t0
-    value = N * (N - 1) * steps / el
+    value = pairs / el
+    sample = ("force loop of the N=16384 workload over %d rows per step (%d ordered pairs), rotating through "
+              "all rows; MDSystem.cpp CPU path restated bit-exactly in C (oracle/lj_oracle.c), OpenMP over i"
+              % (rows, rows * (N - 1)))
     return {
         "metric": "pair-interactions/s, N=16384, FP32-mixed vs FP64 same GB300 @ force rel err<=1e-5",
-        "impl": "reference", "value": value, "unit": "pair-interactions/s", "n_gpus": world, "steps": steps,
-        "warmup": 1, "ms_per_step": el * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32-storage/f64-temporaries", "data": "synthetic (seeded FCC+jitter)",
-        "config": {"workload": WORKLOAD, "n": N, "rho": RHO, "T": T0, "dt": DT, "ensemble": "TVN"},
+        "impl": "reference", "value": value, "unit": "pair-interactions/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-storage/f64-temporaries",
+        "data": "synthetic (seeded FCC+jitter)", "config": bench_config(world),
         "cpu_baseline": {"value": value, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
-                         "sample": "%d full TVN steps of the N=16384 workload; MDSystem.cpp CPU path restated "
-                                   "bit-exactly in C (oracle/lj_oracle.c), OpenMP over i" % steps},
+                         "sample": sample},
         "e2e": {"value": value, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own sources are not present on this machine; the bit-exact C restatement of "
                 "its CPU path runs instead (pinned to the reference by tests/golden)",

@@ -299,7 +299,11 @@ lj_status lj_schedule_plan(const int32_t* n, int32_t nsys, int32_t block, int32_
  * exit), so n is limited to 16384 (larger n: LJ_ERR_INVALID).  All calls on
  * a device share that array and it keeps the last call's contents: calls
  * whose GPU work overlaps race.  The first call on a device looks up the
- * array's address; make it before any stream capture. */
+ * array's address and the device's SM count; make it before any stream
+ * capture.  Every call reads its results back to the host and synchronises
+ * `stream`, so a call on a stream that is being captured returns
+ * LJ_ERR_UNSUPPORTED and enqueues nothing.  After a cudaDeviceReset the next
+ * call sets the array up again. */
 lj_status lj_forces_static(const float* pos4, float* force4, double* sums, int32_t n, float box,
                            int32_t periodic, void* stream);
 

@@ -27,81 +27,7 @@ namespace ljgb {
 namespace {
 
 constexpr int kRefBins = 256;  // NdNdr2 size (MDSystem.cpp:97)
-constexpr int kBlk = 256;
-
-__global__ void k_ref_bbox(const float4* pos, int n, double* blk) {
-  __shared__ double sh[6][32];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  if (i < n) {
-    const float4 p = pos[i];
-    lo[0] = hi[0] = p.x;
-    lo[1] = hi[1] = p.y;
-    lo[2] = hi[2] = p.z;
-  }
-  for (int c = 0; c < 3; ++c)
-    for (int o = 16; o > 0; o >>= 1) {
-      lo[c] = fmin(lo[c], __shfl_down_sync(0xffffffffu, lo[c], o));
-      hi[c] = fmax(hi[c], __shfl_down_sync(0xffffffffu, hi[c], o));
-    }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0)
-    for (int c = 0; c < 3; ++c) {
-      sh[c][warp] = lo[c];
-      sh[3 + c][warp] = hi[c];
-    }
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int c = 0; c < 3; ++c) {
-      double a = 1e300, b = -1e300;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-        a = fmin(a, sh[c][w]);
-        b = fmax(b, sh[3 + c][w]);
-      }
-      blk[(size_t)blockIdx.x * 8 + c] = a;
-      blk[(size_t)blockIdx.x * 8 + 3 + c] = b;
-    }
-}
-
-// One thread: frame of the fixed-point shadow (eps = sigma = 1).
-__global__ void k_ref_frame(const double* blk, int nb, int periodic, double L, DevScalars* sc) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double origin[3] = {0, 0, 0};
-  double P = L;
-  if (!periodic) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int b = 0; b < nb; ++b)
-      for (int c = 0; c < 3; ++c) {
-        lo[c] = fmin(lo[c], blk[(size_t)b * 8 + c]);
-        hi[c] = fmax(hi[c], blk[(size_t)b * 8 + 3 + c]);
-      }
-    double ext = 0;
-    for (int c = 0; c < 3; ++c) {
-      ext = fmax(ext, hi[c] - lo[c]);
-      origin[c] = lo[c];
-    }
-    P = 2.002 * ext + 1e-3;
-  }
-  for (int c = 0; c < 3; ++c) sc->origin[c] = origin[c];
-  sc->P = P;
-  sc->invP = 1.0 / P;
-  const double ks = P / 4294967296.0;
-  sc->k2 = (float)(ks * ks);
-  sc->k2inv = (float)(1.0 / (ks * ks));
-  sc->fscale = 4.0 * ks;
-}
-
-__global__ void k_ref_quantize(const float4* pos, int n, const DevScalars* sc, int4* q) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 p = pos[i];
-  int4 r;
-  r.x = fixed_coord(p.x, sc->origin[0], sc->invP);
-  r.y = fixed_coord(p.y, sc->origin[1], sc->invP);
-  r.z = fixed_coord(p.z, sc->origin[2], sc->invP);
-  r.w = 0;
-  q[i] = r;
-}
+constexpr int kBlk = kFloat4Threads;
 
 // Force[i] = (F, sum_j r^-12 - r^-6); block partial of sum_j s r^2.
 __global__ void k_ref_reduce(const float* partial, const BlockInfo* blocks, int bi_threads, const DevScalars* sc,
@@ -255,14 +181,9 @@ bool calc_forces(float* Pos, float* Force, float* host_pressure, int n, float L,
   if (!ensure_ctx(n, block_size > 0 ? block_size : 128)) return false;
   CompatCtx& c = g_ctx;
   const float4* pos = reinterpret_cast<const float4*>(Pos);
-  if (!periodic) {
-    k_ref_bbox<<<c.nb_bbox, kBlk, 0, c.stream>>>(pos, n, c.blk);
-    REF_CHECK(cudaGetLastError());
-  }
-  k_ref_frame<<<1, 32, 0, c.stream>>>(c.blk, c.nb_bbox, periodic, (double)L, c.sc);
-  REF_CHECK(cudaGetLastError());
-  k_ref_quantize<<<c.nb_bbox, kBlk, 0, c.stream>>>(pos, n, c.sc, c.q);
-  REF_CHECK(cudaGetLastError());
+  if (!periodic) REF_CHECK(launch_float4_bbox(pos, n, c.blk, c.stream));
+  REF_CHECK(launch_float4_frame(c.blk, c.nb_bbox, periodic, (double)L, c.sc, nullptr, c.stream));
+  REF_CHECK(launch_float4_quantize(pos, n, c.sc, c.q, c.stream));
   PairArgs a{};
   a.q = c.q;
   a.blocks = c.blocks;
@@ -388,3 +309,107 @@ int lj_reference_abi_status(void) { return g_status; }
 const char* lj_reference_abi_error(void) { return g_error.c_str(); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Fixed-point shadow of caller-owned float4 positions, shared by the
+// reference ABI above and the allocation-free force entry point
+// (lj_noalloc.cu).
+// ---------------------------------------------------------------------------
+namespace ljgb {
+namespace {
+
+// Per-CTA bounding box of kFloat4Threads positions: blk[b*8 + 0..2] = min,
+// blk[b*8 + 3..5] = max.
+__global__ void k_float4_bbox(const float4* pos, int n, double* blk) {
+  __shared__ double sh[6][32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  if (i < n) {
+    const float4 p = pos[i];
+    lo[0] = hi[0] = p.x;
+    lo[1] = hi[1] = p.y;
+    lo[2] = hi[2] = p.z;
+  }
+  for (int c = 0; c < 3; ++c)
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fmin(lo[c], __shfl_down_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmax(hi[c], __shfl_down_sync(0xffffffffu, hi[c], o));
+    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int c = 0; c < 3; ++c) {
+      sh[c][warp] = lo[c];
+      sh[3 + c][warp] = hi[c];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; ++c) {
+      double a = 1e300, b = -1e300;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        a = fmin(a, sh[c][w]);
+        b = fmax(b, sh[3 + c][w]);
+      }
+      blk[(size_t)blockIdx.x * 8 + c] = a;
+      blk[(size_t)blockIdx.x * 8 + 3 + c] = b;
+    }
+}
+
+// One thread: frame of the fixed-point shadow (eps = sigma = 1).  Periodic:
+// origin 0, period L.  Otherwise the bounding box's low corner and a period
+// of twice its largest extent, so no separation wraps.  Clears *status when
+// given.
+__global__ void k_float4_frame(const double* blk, int nb, int periodic, double L, DevScalars* sc, int* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double origin[3] = {0, 0, 0};
+  double P = L;
+  if (!periodic) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int b = 0; b < nb; ++b)
+      for (int c = 0; c < 3; ++c) {
+        lo[c] = fmin(lo[c], blk[(size_t)b * 8 + c]);
+        hi[c] = fmax(hi[c], blk[(size_t)b * 8 + 3 + c]);
+      }
+    double ext = 0;
+    for (int c = 0; c < 3; ++c) {
+      ext = fmax(ext, hi[c] - lo[c]);
+      origin[c] = lo[c];
+    }
+    P = 2.002 * ext + 1e-3;
+  }
+  for (int c = 0; c < 3; ++c) sc->origin[c] = origin[c];
+  sc->P = P;
+  sc->invP = 1.0 / P;
+  const double ks = P / 4294967296.0;
+  sc->k2 = (float)(ks * ks);
+  sc->k2inv = (float)(1.0 / (ks * ks));
+  sc->fscale = 4.0 * ks;
+  if (status) *status = 0;
+}
+
+__global__ void k_float4_quantize(const float4* pos, int n, const DevScalars* sc, int4* q) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos[i];
+  q[i] = make_int4(fixed_coord(p.x, sc->origin[0], sc->invP), fixed_coord(p.y, sc->origin[1], sc->invP),
+                   fixed_coord(p.z, sc->origin[2], sc->invP), 0);
+}
+
+}  // namespace
+
+cudaError_t launch_float4_bbox(const float4* pos, int n, double* blk, cudaStream_t st) {
+  k_float4_bbox<<<(n + kFloat4Threads - 1) / kFloat4Threads, kFloat4Threads, 0, st>>>(pos, n, blk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_float4_frame(const double* blk, int nb, int periodic, double L, DevScalars* sc, int* status,
+                                cudaStream_t st) {
+  k_float4_frame<<<1, 32, 0, st>>>(blk, nb, periodic, L, sc, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_float4_quantize(const float4* pos, int n, const DevScalars* sc, int4* q, cudaStream_t st) {
+  k_float4_quantize<<<(n + kFloat4Threads - 1) / kFloat4Threads, kFloat4Threads, 0, st>>>(pos, n, sc, q);
+  return cudaGetLastError();
+}
+
+}  // namespace ljgb

@@ -118,6 +118,16 @@ cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t
 cudaError_t launch_tvn_close(const StateArgs& s, int nblocks, int bi, cudaStream_t st);
 cudaError_t launch_obs_finalize(const StateArgs& s, int nsys, cudaStream_t st);
 
+// Fixed-point shadow of caller-owned float4 positions (lj_compat.cu), for the
+// reference ABI and the allocation-free force entry point.  bbox writes one
+// 8-double partial per kFloat4Threads positions (grid = ceil(n / 256)); frame
+// reads nb such partials (non-periodic boxes) and clears *status if given.
+constexpr int kFloat4Threads = 256;
+cudaError_t launch_float4_bbox(const float4* pos, int n, double* blk, cudaStream_t st);
+cudaError_t launch_float4_frame(const double* blk, int nb, int periodic, double L, DevScalars* sc, int* status,
+                                cudaStream_t st);
+cudaError_t launch_float4_quantize(const float4* pos, int n, const DevScalars* sc, int4* q, cudaStream_t st);
+
 // Headless particle image (lj_render.cu): splat + shade into rgba (device).
 cudaError_t launch_render(const double* x, int npad, int p0, int n, int axis, int W, int H, double L, double R,
                           unsigned long long* key, uint8_t* rgba, cudaStream_t st);

@@ -17,8 +17,17 @@
 //  * all calls on a device share the one array and it keeps the last call's
 //    contents: calls whose GPU work overlaps (two host threads, or two
 //    streams) race and corrupt each other's results; serialise them;
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress); make that first call before any stream capture.
+//  * every call looks up the array's device address on the current device
+//    (cudaGetSymbolAddress; the host-side name of a __device__ array is not a
+//    device pointer), and the first call on a device also reads its SM count
+//    and checks the kernel shape this file's scratch layout is sized for;
+//    make that first call before any stream capture begins;
+//  * every call ends by reading its status word and sums back to the host
+//    on `stream` and synchronising it, so a call on a stream that is being
+//    captured is rejected with LJ_ERR_UNSUPPORTED before anything is enqueued;
+//  * the cached work schedule belongs to the array's current address: after
+//    a cudaDeviceReset the next call finds a new address (or the same one
+//    with the schedule gone) and uploads the schedule again.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -40,7 +49,7 @@ constexpr int kShape = 0;                         // kShapes[0] = {128, 256, 3}
 constexpr int kMaxBlocks = kStaticMaxParticles / kBI;
 constexpr int kMaxCtas = 1536;
 constexpr int kMaxSegs = kMaxCtas + kMaxBlocks;
-constexpr int kBboxThreads = 256;
+constexpr int kBboxThreads = kFloat4Threads;
 constexpr int kMaxBbox = kStaticMaxParticles / kBboxThreads;
 
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -60,77 +69,6 @@ constexpr size_t kScratchBytes = kOffPartial + align256(sizeof(float) * 5 * kBI 
 
 // The scratch (about 4.4 MB per GPU).
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
-
-__global__ void k_static_bbox(const float4* pos, int n, double* blk) {
-  __shared__ double sh[6][32];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  if (i < n) {
-    const float4 p = pos[i];
-    lo[0] = hi[0] = p.x;
-    lo[1] = hi[1] = p.y;
-    lo[2] = hi[2] = p.z;
-  }
-  for (int c = 0; c < 3; ++c)
-    for (int o = 16; o > 0; o >>= 1) {
-      lo[c] = fmin(lo[c], __shfl_down_sync(0xffffffffu, lo[c], o));
-      hi[c] = fmax(hi[c], __shfl_down_sync(0xffffffffu, hi[c], o));
-    }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0)
-    for (int c = 0; c < 3; ++c) {
-      sh[c][warp] = lo[c];
-      sh[3 + c][warp] = hi[c];
-    }
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int c = 0; c < 3; ++c) {
-      double a = 1e300, b = -1e300;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-        a = fmin(a, sh[c][w]);
-        b = fmax(b, sh[3 + c][w]);
-      }
-      blk[(size_t)blockIdx.x * 8 + c] = a;
-      blk[(size_t)blockIdx.x * 8 + 3 + c] = b;
-    }
-}
-
-// Frame of the fixed-point shadow (eps = sigma = 1) and a cleared status word.
-__global__ void k_static_frame(const double* blk, int nb, int periodic, double L, DevScalars* sc, int* status) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double origin[3] = {0, 0, 0};
-  double P = L;
-  if (!periodic) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int b = 0; b < nb; ++b)
-      for (int c = 0; c < 3; ++c) {
-        lo[c] = fmin(lo[c], blk[(size_t)b * 8 + c]);
-        hi[c] = fmax(hi[c], blk[(size_t)b * 8 + 3 + c]);
-      }
-    double ext = 0;
-    for (int c = 0; c < 3; ++c) {
-      ext = fmax(ext, hi[c] - lo[c]);
-      origin[c] = lo[c];
-    }
-    P = 2.002 * ext + 1e-3;
-  }
-  for (int c = 0; c < 3; ++c) sc->origin[c] = origin[c];
-  sc->P = P;
-  sc->invP = 1.0 / P;
-  const double ks = P / 4294967296.0;
-  sc->k2 = (float)(ks * ks);
-  sc->k2inv = (float)(1.0 / (ks * ks));
-  sc->fscale = 4.0 * ks;
-  *status = 0;
-}
-
-__global__ void k_static_quantize(const float4* pos, int n, const DevScalars* sc, int4* q) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 p = pos[i];
-  q[i] = make_int4(fixed_coord(p.x, sc->origin[0], sc->invP), fixed_coord(p.y, sc->origin[1], sc->invP),
-                   fixed_coord(p.z, sc->origin[2], sc->invP), 0);
-}
 
 // force4[i] = (F, sum_j r^-12 - r^-6); block sums of V and W.
 __global__ void k_static_reduce(const float* partial, const BlockInfo* blocks, const DevScalars* sc, float4* force,
@@ -264,23 +202,35 @@ extern "C" lj_status lj_forces_static(const float* pos4, float* force4, double* 
     return (lj_status)static_fail(LJ_ERR_INVALID, msg);
   }
   if (periodic && !(box > 0.0f)) return (lj_status)static_fail(LJ_ERR_INVALID, "box must be > 0 for a periodic box");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return (lj_status)static_fail(LJ_ERR_UNSUPPORTED, "the stream is being captured (each call reads its results "
+                                  "back to the host and synchronises the stream)");
   std::lock_guard<std::mutex> lk(g_static_mu);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return (lj_status)static_fail(LJ_ERR_NO_DEVICE, "no current CUDA device");
-  cudaStream_t st = (cudaStream_t)stream;
-  // Once per device: the device address of the scratch array (the host-side
-  // name of a __device__ array is not a device pointer).
+  // The device address of the scratch array on this device.  Looked up on
+  // every call: a cudaDeviceReset by the embedding program gives the module
+  // a new load, and the schedule cached in the array is then gone.
+  void* addr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&addr, g_static_scratch);
+  if (e != cudaSuccess) return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
   if (!g_static_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess) return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
+    // The scratch layout is sized for kShapes[kShape]; refuse to launch if
+    // that table entry no longer is the 128-thread, 256-record shape.
+    if (kShape >= kNumShapes || kShapes[kShape].threads != kBI || kShapes[kShape].tile != kTile)
+      return (lj_status)static_fail(LJ_ERR_INVALID, "pair-kernel shape 0 is not the 128-thread / 256-record "
+                                    "shape the static scratch layout is sized for");
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
-    g_static_ptr[dev] = static_cast<unsigned char*>(p);
-    g_static_plan_n[dev] = -1;
     g_static_sms[dev] = sms;
+  }
+  if (g_static_ptr[dev] != static_cast<unsigned char*>(addr)) {
+    g_static_ptr[dev] = static_cast<unsigned char*>(addr);
+    g_static_plan_n[dev] = -1;
   }
   unsigned char* base = g_static_ptr[dev];
   DevScalars* sc = reinterpret_cast<DevScalars*>(base + kOffFrame);
@@ -296,13 +246,14 @@ extern "C" lj_status lj_forces_static(const float* pos4, float* force4, double* 
 
   // The work schedule depends only on n (and the device); it stays in the
   // array until a call with another n replaces it.
-  cudaError_t e;
   if (g_static_plan_n[dev] != n) {
     int per_sm = 0;
     e = pair_occupancy(0, kShape, &per_sm);
     if (e != cudaSuccess) return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
     plan_static(n, g_static_sms[dev] * per_sm, &g_static_plan);
     const StaticPlan& p = g_static_plan;
+    if (p.G > kMaxCtas || p.nseg > kMaxSegs || p.nblocks > kMaxBlocks)
+      return (lj_status)static_fail(LJ_ERR_INVALID, "work schedule exceeds the static scratch layout");
     if ((e = cudaMemcpyAsync(blocks, p.blocks, sizeof(BlockInfo) * p.nblocks, cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(cta_begin, p.cta_begin, sizeof(int) * (p.G + 1), cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(cta_block, p.cta_block, sizeof(int) * p.G, cudaMemcpyHostToDevice, st)) ||
@@ -316,9 +267,11 @@ extern "C" lj_status lj_forces_static(const float* pos4, float* force4, double* 
   const int G = g_static_G[dev], nblocks = g_static_nblocks[dev];
   const float4* pos = reinterpret_cast<const float4*>(pos4);
   const int nbb = (n + kBboxThreads - 1) / kBboxThreads;
-  if (!periodic) k_static_bbox<<<nbb, kBboxThreads, 0, st>>>(pos, n, blk);
-  k_static_frame<<<1, 32, 0, st>>>(blk, nbb, periodic ? 1 : 0, (double)box, sc, status);
-  k_static_quantize<<<nbb, kBboxThreads, 0, st>>>(pos, n, sc, q);
+  if (!periodic && (e = launch_float4_bbox(pos, n, blk, st)) != cudaSuccess)
+    return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
+  if ((e = launch_float4_frame(blk, nbb, periodic ? 1 : 0, (double)box, sc, status, st)) != cudaSuccess ||
+      (e = launch_float4_quantize(pos, n, sc, q, st)) != cudaSuccess)
+    return (lj_status)static_fail(LJ_ERR_CUDA, cudaGetErrorString(e));
   PairArgs a{};
   a.q = q;
   a.blocks = blocks;

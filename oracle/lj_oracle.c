@@ -26,6 +26,13 @@
  *   emu_*  Bit-exact emulation of the integer/histogram decisions the device
  *          makes (fixed-point positions, FP32 r^2 bins, FP64 speed bins), so
  *          histogram counts can be compared exactly.
+ *
+ *   init_* The seeded initial state of the benchmark workloads (lattice,
+ *          jitter, Maxwell speeds by the reference's rejection sampler
+ *          MDSystem.cpp:36-53 and :147-181, zero momentum :183-216, exact T0
+ *          :375-389, drawn from a xoshiro256** stream), so the CPU baseline
+ *          starts from the same state as the GPU arm without loading the
+ *          product library.
  */
 #include <math.h>
 #include <stdint.h>
@@ -115,6 +122,22 @@ static void r32_force_row(const r32_state* s, float* frc, int i, double* V, doub
   frc[i] *= 4;
   frc[i + 1] *= 4;
   frc[i + 2] *= 4;
+}
+
+/* The same j-loop for rows [i0, i1) only, split over nthreads OpenMP threads:
+ * a bounded sample of one force evaluation ((i1 - i0)(N - 1) ordered pairs)
+ * for timing.  Writes those rows of frc; returns sum_i V_i of the rows. */
+double r32_force_rows(const r32_state* s, float* frc, int i0, int i1, int nthreads) {
+  double Vsum = 0.;
+  int nt = nthreads > 1 ? nthreads : 1;
+#pragma omp parallel for num_threads(nt) schedule(static) reduction(+ : Vsum)
+  for (int p = i0; p < i1; ++p) {
+    double V = 0., P = 0., Ps = 0.;
+    int hist[256] = {0};
+    r32_force_row(s, frc, 4 * p, &V, &P, &Ps, hist);
+    Vsum += V;
+  }
+  return Vsum;
 }
 
 /* MDSystem::CalculateForces(float*), CPU branch (MDSystem.cpp:252-310). */
@@ -564,4 +587,104 @@ void emu_velocity_counts(int N, const double* vel, double step, int nb, uint64_t
     double b = floor(sqrt(s) / step);
     if (b < (double)nb) counts[(int)b]++;
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* init_*: seeded initial state (the draws lj_sample_initial_state makes)   */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  uint64_t s[4];
+} init_rng;
+
+static uint64_t init_splitmix(uint64_t* x) {
+  uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static uint64_t init_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+/* xoshiro256** (Blackman & Vigna) */
+static uint64_t init_next(init_rng* r) {
+  uint64_t* s = r->s;
+  const uint64_t out = init_rotl(s[1] * 5, 7) * 9;
+  const uint64_t t = s[1] << 17;
+  s[2] ^= s[0];
+  s[3] ^= s[1];
+  s[1] ^= s[2];
+  s[0] ^= s[3];
+  s[2] ^= t;
+  s[3] = init_rotl(s[3], 45);
+  return out;
+}
+
+static double init_uniform(init_rng* r) { return (double)(init_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+
+/* pos, vel: (n, 3) doubles; *L_out = cbrt(n / density).  lattice 0: simple
+ * cubic, 1: FCC; sites filled in lattice order (x fastest), cell-centred;
+ * uniform jitter of +-jitter. */
+int init_sample_state(int n, double density, double T0, int lattice, double jitter, uint64_t seed, double* pos,
+                      double* vel, double* L_out) {
+  if (n < 1 || !(density > 0) || !(T0 >= 0)) return 1;
+  const double L = cbrt((double)n / density);
+  *L_out = L;
+  init_rng rng;
+  uint64_t x = seed;
+  for (int k = 0; k < 4; ++k) rng.s[k] = init_splitmix(&x);
+  if (lattice == 0) {
+    const int ns = (int)ceil(cbrt((double)n) - 1e-12);
+    const int side = (ns * ns * ns < n) ? ns + 1 : ns;
+    const double dL = L / side;
+    for (int i = 0; i < n; ++i) {
+      pos[3 * i + 0] = (i % side + 0.5) * dL;
+      pos[3 * i + 1] = ((i / side) % side + 0.5) * dL;
+      pos[3 * i + 2] = (i / (side * side) + 0.5) * dL;
+    }
+  } else {
+    static const double basis[4][3] = {{0, 0, 0}, {0.5, 0.5, 0}, {0.5, 0, 0.5}, {0, 0.5, 0.5}};
+    int nc = (int)ceil(cbrt(n / 4.0) - 1e-12);
+    while (4 * nc * nc * nc < n) ++nc;
+    const double a = L / nc;
+    for (int i = 0; i < n; ++i) {
+      const int c = i / 4, b = i % 4;
+      pos[3 * i + 0] = (c % nc + basis[b][0] + 0.25) * a;
+      pos[3 * i + 1] = ((c / nc) % nc + basis[b][1] + 0.25) * a;
+      pos[3 * i + 2] = (c / (nc * nc) + basis[b][2] + 0.25) * a;
+    }
+  }
+  if (jitter > 0)
+    for (int k = 0; k < 3 * n; ++k) pos[k] += (2.0 * init_uniform(&rng) - 1.0) * jitter;
+  /* speed u = -ln(alpha), alpha accepted with probability
+     prob(alpha) / probmax, prob(alpha) = ln^2(alpha) exp(-ln^2 alpha) / alpha */
+  for (int i = 0; i < n; ++i) {
+    double alpha;
+    for (;;) {
+      do alpha = init_uniform(&rng);
+      while (alpha == 0.0);
+      const double eta = init_uniform(&rng) * 1.2;
+      const double tl = -log(alpha);
+      if (eta < tl * tl * exp(-tl * tl) / alpha) break;
+    }
+    const double speed = sqrt(2.0 * T0) * (-log(alpha));
+    const double cth = 2.0 * init_uniform(&rng) - 1.0;
+    const double ph = 2.0 * ORACLE_PI * init_uniform(&rng);
+    const double sth = sqrt(1.0 - cth * cth);
+    vel[3 * i + 0] = speed * sth * cos(ph);
+    vel[3 * i + 1] = speed * sth * sin(ph);
+    vel[3 * i + 2] = speed * cth;
+  }
+  double P[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) P[c] += vel[3 * i + c];
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) vel[3 * i + c] -= P[c] / n;
+  double s2 = 0;
+  for (int k = 0; k < 3 * n; ++k) s2 += vel[k] * vel[k];
+  const double Tkin = s2 / 3.0 / n;
+  if (Tkin > 0) {
+    const double f = sqrt(T0 / Tkin);
+    for (int k = 0; k < 3 * n; ++k) vel[k] *= f;
+  }
+  return 0;
 }

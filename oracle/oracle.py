@@ -60,6 +60,18 @@ def build_ref(ref_dir: str = None) -> bool:
     return os.path.exists(REF_PATH)
 
 
+def sample_state(n, density, temperature, lattice=1, jitter=0.0, seed=1):
+    """The seeded initial state of a workload ((n,3) positions, velocities,
+    box side): lattice 0 = simple cubic, 1 = FCC."""
+    pos = np.zeros((n, 3))
+    vel = np.zeros((n, 3))
+    L = C.c_double()
+    if lib().init_sample_state(int(n), float(density), float(temperature), int(lattice), float(jitter), int(seed),
+                               pos, vel, C.byref(L)):
+        raise ValueError("bad initial-state arguments")
+    return pos, vel, L.value
+
+
 class _R32State(C.Structure):
     _fields_ = [("N", C.c_int), ("T0", C.c_double), ("rho", C.c_double), ("canonical", C.c_int),
                 ("bc", C.c_int), ("L", C.c_double), ("t", C.c_double), ("U", C.c_double),
@@ -79,9 +91,14 @@ def lib():
         build()
         L = C.CDLL(LIB_PATH)
         P = C.POINTER(_R32State)
+        L.init_sample_state.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_uint64,
+                                        _f64p, _f64p, C.POINTER(C.c_double)]
+        L.init_sample_state.restype = C.c_int
         L.r32_rdf_dr2.argtypes = [C.c_int]
         L.r32_rdf_dr2.restype = C.c_float
         L.r32_calculate_forces.argtypes = [P, C.c_void_p, C.c_int]
+        L.r32_force_rows.argtypes = [P, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.r32_force_rows.restype = C.c_double
         L.r32_calculate_parameters.argtypes = [P]
         L.r32_kinetic_temperature.argtypes = [P, C.c_void_p]
         L.r32_kinetic_temperature.restype = C.c_double
@@ -144,6 +161,10 @@ class R32System:
 
     def calculate_forces(self, nthreads=1):
         lib().r32_calculate_forces(C.byref(self.s), self.frc.ctypes.data, int(nthreads))
+
+    def force_rows(self, i0, i1, nthreads=1):
+        """The force loop over rows [i0, i1) only (a timing sample)."""
+        return lib().r32_force_rows(C.byref(self.s), self.frc.ctypes.data, int(i0), int(i1), int(nthreads))
 
     def calculate_parameters(self):
         lib().r32_calculate_parameters(C.byref(self.s))

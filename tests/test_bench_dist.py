@@ -81,3 +81,26 @@ def test_clock_samples_kept_only_inside_the_timed_region():
     assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
     assert s["reasons"] == ["sw_power_cap"]
     assert s["region_s"] == pytest.approx(1.0)
+
+
+def test_reference_arm_line_without_the_product_library():
+    """`bench.py --impl reference` (rank 0, one process): K timed steps and W
+    warm-up steps as asked, the same config as the GPU arm, and the product
+    library never loaded into the process."""
+    import json
+    import subprocess
+    import sys
+    code = ("import sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '3', '--warmup', '1'];"
+            "sys.path.insert(0, %r); import bench; bench.main();"
+            "maps = open('/proc/self/maps').read();"
+            "print(json.dumps({'lj_loaded': 'liblj_gb300' in maps, 'ljgb_imported': 'ljgb' in sys.modules}))"
+            % REPO)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert out.returncode == 0, out.stderr
+    lines = [json.loads(x) for x in out.stdout.splitlines() if x.startswith("{")]
+    line, probe = lines[0], lines[-1]
+    import bench
+    assert line["impl"] == "reference" and line["steps"] == 3 and line["warmup"] == 1
+    assert line["config"] == bench.bench_config(1)
+    assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
+    assert probe == {"lj_loaded": False, "ljgb_imported": False}

@@ -173,3 +173,20 @@ def test_emulated_velocity_histogram(oracle_mod):
     c = oracle_mod.emu_velocity_counts(vel, 0.12, 101)
     ref = np.bincount(np.floor(np.sqrt(np.sum(vel * vel, 1)) / 0.12).astype(int), minlength=200)[:101]
     assert np.array_equal(c.astype(np.int64), ref)
+
+
+@pytest.mark.parametrize("n,rho,T0,lattice,jitter,seed", [(16384, 0.85, 1.0, 1, 0.02, 2), (400, 0.05, 1.4, 0, 0.05, 400),
+                                                          (262144, 1.1, 1.0, 1, 0.01, 262144), (1000, 0.3, 2.0, 0, 0.0, 9)])
+def test_oracle_initial_state_is_the_library_sampler(ljlib, n, rho, T0, lattice, jitter, seed):
+    """oracle.sample_state (the CPU baseline's start, drawn without loading
+    the product library) gives the state lj_sample_initial_state draws."""
+    import ljgb
+    import oracle
+    cfg = ljgb.config(n=n, density=rho, temperature=T0, lattice=lattice, jitter=jitter, seed=seed)
+    p, v = ljgb.sample_initial_state(cfg)
+    po, vo, L = oracle.sample_state(n, rho, T0, lattice, jitter, seed)
+    assert L == pytest.approx((n / rho) ** (1 / 3), rel=1e-14)
+    # identical draws; the last bits may differ where a compiler contracts a
+    # multiply-add on one side only
+    assert np.abs(p - po).max() <= 1e-12 * L
+    assert np.abs(v - vo).max() <= 1e-12

@@ -103,6 +103,59 @@ def test_static_dense_box_two_calls(ljlib):
     ljlib.deleteArray(d_pos)
 
 
+@pytest.mark.parametrize("n", [16384, 16383])
+def test_static_at_the_size_limit_against_fp64_oracle(ljlib, oracle_mod, n):
+    """At the documented maximum (and one below, a ragged last i-block) the
+    scratch regions are fullest.  Two calls in a row against calculateNForces
+    and, on a seeded subset of 2048 rows, against the FP64 oracle on the same
+    float positions (force gate |dF_i| <= 1e-5 max(|F_i|, rms|F|), median
+    |dF_i|/|F_i| <= 1e-5; sum_j (r^-12 - r^-6) to 1e-5 of its largest)."""
+    fn = bind(ljlib)
+    pos, _, L = U.lattice_state(n, 0.85, 1.0, "fcc", 0.02, seed=n)
+    pos4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = pos
+    box = np.float32(L)
+    d_pos = device_array(ljlib, n)
+    ljlib.copyArrayToDevice(d_pos, pos4.ctypes.data, n)
+    f_ref, pressure = run_existing(ljlib, d_pos, n, box, True)
+    i0 = int(np.random.default_rng(n).integers(0, n - 2048))
+    r = oracle_mod.f64_forces(pos4[:, :3].astype(np.float64), float(box), True, rows=(i0, i0 + 2048))
+    for _ in range(2):
+        rc, f_static, sums = run_static(ljlib, fn, d_pos, n, box, True)
+        assert rc == 0
+        compare(f_static, f_ref, sums, pressure)
+        err = U.force_errors(f_static[i0:i0 + 2048, :3].astype(np.float64), r["F"])
+        print("lj_forces_static n=%d rows %d..%d vs FP64 oracle: %s" % (n, i0, i0 + 2048, err))
+        assert err["gate_max"] <= 1e-5 and err["rel_median"] <= 1e-5
+        # Force.w = sum_j (r^-12 - r^-6); the oracle's e_i = 4 sum_j (r^-12 - r^-6)
+        w = f_static[i0:i0 + 2048, 3].astype(np.float64)
+        assert np.abs(4.0 * w - r["e"]).max() <= 1e-5 * np.abs(r["e"]).max()
+    ljlib.deleteArray(d_pos)
+
+
+def test_static_rejects_a_capturing_stream(ljlib):
+    """Each call reads its results back and synchronises its stream, which a
+    stream capture cannot hold: on a capturing stream the call returns
+    LJ_ERR_UNSUPPORTED and enqueues nothing, so the caller's capture stays
+    valid."""
+    torch = pytest.importorskip("torch")
+    fn = bind(ljlib)
+    n = 256
+    d_pos, d_frc = device_array(ljlib, n), device_array(ljlib, n)
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    x = torch.zeros(4, device="cuda")
+    with torch.cuda.graph(g, stream=side):
+        rc = fn(d_pos, d_frc, None, n, C.c_float(10.0), 1, C.c_void_p(side.cuda_stream))
+        x += 1.0
+    assert rc == 6  # LJ_ERR_UNSUPPORTED
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x.sum()) == 4.0
+    ljlib.deleteArray(d_pos)
+    ljlib.deleteArray(d_frc)
+
+
 def test_static_rejects_oversized_box(ljlib):
     fn = bind(ljlib)
     d = device_array(ljlib, 4)
