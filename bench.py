@@ -381,14 +381,8 @@ def ref_gpu_kernel(torch, ljgb, dev, flush, pair_ms, steps=20, block=256):
     (FP32 nbody tiles, lround minimum image, a global RDF atomic per pair),
     timed on the bench state: informational, beside the library's pair
     kernel."""
-    import ctypes as C
-    import ljgb.build as B
-    lib = C.CDLL(B.COMPARATOR_LIB)
-    lib.ljref_scratch_bytes.restype = C.c_size_t
-    lib.ljref_scratch_bytes.argtypes = [C.c_int, C.c_int]
-    lib.ljref_forces.restype = C.c_int
-    lib.ljref_forces.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_float, C.c_int,
-                                 C.c_void_p, C.c_void_p]
+    import comparator
+    lib = comparator.load()
     s = make_system(ljgb, 0, dev)
     pos, _, _ = s.get_state()
     L = s.L

@@ -60,10 +60,10 @@ def _compile(src: str, verbose: bool) -> str:
 
 
 def _stale() -> bool:
-    if not os.path.exists(LIB_PATH) or not os.path.exists(COMPARATOR_LIB):
+    if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    for d in (CSRC, INCLUDE, os.path.join(PKG_DIR, "tasks"), os.path.join(PKG_DIR, "comparator")):
+    for d in (CSRC, INCLUDE, os.path.join(PKG_DIR, "tasks")):
         for root, _, files in os.walk(d):
             for f in files:
                 if os.path.getmtime(os.path.join(root, f)) > t:
@@ -99,30 +99,8 @@ def _build_into(lib_path: str, verbose: bool) -> str:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, lib_path)
     if lib_path == LIB_PATH:
-        with cf.ThreadPoolExecutor(max_workers=2) as ex:
-            jobs = [ex.submit(build_tasks), ex.submit(build_comparator)]
-            for j in jobs:
-                j.result()
+        build_tasks()
     return lib_path
-
-
-COMPARATOR_DIR = os.path.join(PKG_DIR, "comparator")
-COMPARATOR_LIB = os.path.join(COMPARATOR_DIR, "libljref_nbody.so")
-
-
-def build_comparator() -> str:
-    """The timing comparator (the reference's GPU force kernel restated,
-    comparator/ref_nbody.cu) as its own shared library; the product library
-    does not link it."""
-    tmp = COMPARATOR_LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-                             os.path.join(COMPARATOR_DIR, "ref_nbody.cu"), "-o", tmp, "-lcudart_static", "-lrt",
-                             "-lpthread", "-ldl"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("comparator build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, COMPARATOR_LIB)
-    return COMPARATOR_LIB
 
 
 TASKS = {"ljgb-run-isotherm": "run_isotherm.cpp", "ljgb-run-fluctuations": "run_fluctuations.cpp",

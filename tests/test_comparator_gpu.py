@@ -1,5 +1,5 @@
 """The timing comparator (the reference's GPU force kernel restated in
-lennard-jones-cuda_gb300/comparator/ref_nbody.cu) computes what the
+comparator/ref_nbody.cu) computes what the
 reference's kernel computes: forces against the FP64 oracle at FP32
 accuracy, Force.w = sum_j (r^-12 - r^-6), the virial sum W/6 and the
 clamped r^2 RDF over all ordered pairs."""
@@ -15,15 +15,8 @@ pytestmark = pytest.mark.gpu
 
 
 def _lib():
-    import ljgb.build as B
-    B.build()
-    lib = C.CDLL(B.COMPARATOR_LIB)
-    lib.ljref_scratch_bytes.restype = C.c_size_t
-    lib.ljref_scratch_bytes.argtypes = [C.c_int, C.c_int]
-    lib.ljref_forces.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_float, C.c_int,
-                                 C.c_void_p, C.c_void_p]
-    lib.ljref_results.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
-    return lib
+    import comparator
+    return comparator.load()
 
 
 @pytest.mark.parametrize("n,block", [(2000, 256), (1000, 128), (300, 512)])
