@@ -390,6 +390,18 @@ lj_status lj_adjoint_backward(lj_adjoint* adj, double* d_epsilon, double* d_sigm
 void* lj_host_alloc(size_t bytes);
 void lj_host_free(void* ptr);
 
+/* Out-of-memory testing hook (host side; no counterpart in the reference,
+ * whose checkCudaErrors(cudaMalloc(...)) exits the process on a failed
+ * allocation, MDSystem.cu:167-173).  after >= 0: the next `after` device or
+ * page-locked host allocations of this library succeed and every later one
+ * fails with LJ_ERR_OUT_OF_MEMORY (the reference ABI: status
+ * LJ_ERR_OUT_OF_MEMORY) without calling CUDA, until lj_debug_fail_allocations(-1)
+ * turns the hook off.  Process-wide.  A call that fails this way leaves its
+ * handle as it was: creation frees what it had allocated, a new schedule,
+ * histogram range table, record ring or counter table replaces the old one
+ * only once complete, and an interrupted autotune puts the state back. */
+lj_status lj_debug_fail_allocations(int64_t after);
+
 /* Library version string and the device architecture it was built for. */
 const char* lj_version(void);
 

@@ -250,8 +250,12 @@ struct DBuf {
     if (p) cudaFree(p);
     p = nullptr;
     n = 0;
-    cudaError_t e = cudaMalloc(&p, sizeof(T) * (count ? count : 1));
-    if (e == cudaSuccess) n = count;
+    void* q = nullptr;
+    cudaError_t e = device_alloc(&q, sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess) {
+      p = static_cast<T*>(q);
+      n = count;
+    }
     return e;
   }
   void free() {

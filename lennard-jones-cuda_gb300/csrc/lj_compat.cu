@@ -101,7 +101,7 @@ std::string g_error;
 
 bool record(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return true;
-  g_status = LJ_ERR_CUDA;
+  g_status = e == cudaErrorMemoryAllocation ? LJ_ERR_OUT_OF_MEMORY : LJ_ERR_CUDA;
   g_error = std::string(what) + ": " + cudaGetErrorString(e);
   std::fprintf(stderr, "lj_gb300 reference ABI: %s\n", g_error.c_str());
   return false;
@@ -141,31 +141,40 @@ bool ensure_ctx(int n, int block_hint) {
   c.n = n;
   c.shape = shape;
   c.nb_bbox = (n + kBlk - 1) / kBlk;
-  // A blocking stream: the reference's ABI is synchronous and its copies
-  // (copyArrayToDevice, cudaMemcpy on the legacy stream) must be ordered
-  // before this stream's kernels; a pageable cudaMemcpy can return before
-  // its DMA has landed.
-  REF_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamDefault));
-  const int nb = (int)s.blocks.size();
-  REF_CHECK(cudaMalloc(&c.q, sizeof(int4) * n));
-  REF_CHECK(cudaMalloc(&c.sc, sizeof(DevScalars)));
-  REF_CHECK(cudaMalloc(&c.blocks, sizeof(BlockInfo) * nb));
-  REF_CHECK(cudaMalloc(&c.ctb, sizeof(int) * (s.G + 1)));
-  REF_CHECK(cudaMalloc(&c.clo, sizeof(int) * (s.G + 1)));
-  REF_CHECK(cudaMalloc(&c.cb, sizeof(int) * s.G));
-  REF_CHECK(cudaMalloc(&c.cj, sizeof(int) * s.G));
-  REF_CHECK(cudaMalloc(&c.partial, sizeof(float) * (size_t)s.nseg * 5 * s.BI));
-  REF_CHECK(cudaMalloc(&c.blk, sizeof(double) * 8 * (size_t)std::max(nb, c.nb_bbox)));
-  REF_CHECK(cudaMalloc(&c.hist, sizeof(unsigned long long) * kRefBins));
-  REF_CHECK(cudaMalloc(&c.status, sizeof(int)));
-  REF_CHECK(cudaMalloc(&c.pressure, sizeof(float)));
-  REF_CHECK(cudaMemset(c.sc, 0, sizeof(DevScalars)));
-  REF_CHECK(cudaMemset(c.status, 0, sizeof(int)));
-  REF_CHECK(cudaMemcpy(c.blocks, s.blocks.data(), sizeof(BlockInfo) * nb, cudaMemcpyHostToDevice));
-  REF_CHECK(cudaMemcpy(c.ctb, s.cta_tile_begin.data(), sizeof(int) * (s.G + 1), cudaMemcpyHostToDevice));
-  REF_CHECK(cudaMemcpy(c.clo, s.cta_lo.data(), sizeof(int) * (s.G + 1), cudaMemcpyHostToDevice));
-  REF_CHECK(cudaMemcpy(c.cb, s.cta_block.data(), sizeof(int) * s.G, cudaMemcpyHostToDevice));
-  REF_CHECK(cudaMemcpy(c.cj, s.cta_jt.data(), sizeof(int) * s.G, cudaMemcpyHostToDevice));
+  // Buffers of the new context; on any failure everything allocated so far
+  // is freed and the layer is left without a context (the next call retries).
+  auto build = [&]() -> bool {
+    // A blocking stream: the reference's ABI is synchronous and its copies
+    // (copyArrayToDevice, cudaMemcpy on the legacy stream) must be ordered
+    // before this stream's kernels; a pageable cudaMemcpy can return before
+    // its DMA has landed.
+    REF_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamDefault));
+    const int nb = (int)s.blocks.size();
+    REF_CHECK(device_alloc((void**)&c.q, sizeof(int4) * n));
+    REF_CHECK(device_alloc((void**)&c.sc, sizeof(DevScalars)));
+    REF_CHECK(device_alloc((void**)&c.blocks, sizeof(BlockInfo) * nb));
+    REF_CHECK(device_alloc((void**)&c.ctb, sizeof(int) * (s.G + 1)));
+    REF_CHECK(device_alloc((void**)&c.clo, sizeof(int) * (s.G + 1)));
+    REF_CHECK(device_alloc((void**)&c.cb, sizeof(int) * s.G));
+    REF_CHECK(device_alloc((void**)&c.cj, sizeof(int) * s.G));
+    REF_CHECK(device_alloc((void**)&c.partial, sizeof(float) * (size_t)s.nseg * 5 * s.BI));
+    REF_CHECK(device_alloc((void**)&c.blk, sizeof(double) * 8 * (size_t)std::max(nb, c.nb_bbox)));
+    REF_CHECK(device_alloc((void**)&c.hist, sizeof(unsigned long long) * kRefBins));
+    REF_CHECK(device_alloc((void**)&c.status, sizeof(int)));
+    REF_CHECK(device_alloc((void**)&c.pressure, sizeof(float)));
+    REF_CHECK(cudaMemset(c.sc, 0, sizeof(DevScalars)));
+    REF_CHECK(cudaMemset(c.status, 0, sizeof(int)));
+    REF_CHECK(cudaMemcpy(c.blocks, s.blocks.data(), sizeof(BlockInfo) * nb, cudaMemcpyHostToDevice));
+    REF_CHECK(cudaMemcpy(c.ctb, s.cta_tile_begin.data(), sizeof(int) * (s.G + 1), cudaMemcpyHostToDevice));
+    REF_CHECK(cudaMemcpy(c.clo, s.cta_lo.data(), sizeof(int) * (s.G + 1), cudaMemcpyHostToDevice));
+    REF_CHECK(cudaMemcpy(c.cb, s.cta_block.data(), sizeof(int) * s.G, cudaMemcpyHostToDevice));
+    REF_CHECK(cudaMemcpy(c.cj, s.cta_jt.data(), sizeof(int) * s.G, cudaMemcpyHostToDevice));
+    return true;
+  };
+  if (!build()) {
+    c.release();
+    return false;
+  }
   c.sched = std::move(s);
   g_ctx = c;
   return true;
@@ -232,13 +241,18 @@ void allocateNBodyArrays(float* vel[2], int numBodies) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_status = 0;
   const size_t bytes = sizeof(float) * 4 * (size_t)numBodies;
-  if (record(cudaMalloc((void**)&vel[0], bytes), "cudaMalloc")) record(cudaMalloc((void**)&vel[1], bytes), "cudaMalloc");
+  vel[0] = vel[1] = nullptr;
+  if (record(device_alloc((void**)&vel[0], bytes), "cudaMalloc") &&
+      !record(device_alloc((void**)&vel[1], bytes), "cudaMalloc")) {
+    cudaFree(vel[0]);
+    vel[0] = nullptr;
+  }
 }
 
 void allocateArray(float** dest, int number) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_status = 0;
-  record(cudaMalloc((void**)dest, sizeof(float) * 4 * (size_t)number), "cudaMalloc");
+  record(device_alloc((void**)dest, sizeof(float) * 4 * (size_t)number), "cudaMalloc");
 }
 
 void deleteNBodyArrays(float* vel[2]) {
@@ -257,7 +271,7 @@ void deleteArray(float* arr) {
 void allocateIntArray(int** dest, int number) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_status = 0;
-  record(cudaMalloc((void**)dest, sizeof(int) * (size_t)number), "cudaMalloc");
+  record(device_alloc((void**)dest, sizeof(int) * (size_t)number), "cudaMalloc");
 }
 
 void deleteIntArray(int* arr) {

@@ -32,6 +32,14 @@ class DeviceGuard {
   cudaError_t err_ = cudaSuccess;
 };
 
+// Every device and page-locked host allocation the library makes goes
+// through these two calls (lj_system.cpp).  lj_debug_fail_allocations arms a
+// host-side countdown that makes them fail with cudaErrorMemoryAllocation
+// without calling CUDA, so the out-of-memory paths can be tested without
+// exhausting a GPU.
+cudaError_t device_alloc(void** p, size_t bytes);
+cudaError_t pinned_alloc(void** p, size_t bytes);
+
 // Device-side status flags (DevScalars::status).
 enum : int {
   LJ_DEVFLAG_TIMEOUT = 1,    // a bounded mbarrier wait gave up

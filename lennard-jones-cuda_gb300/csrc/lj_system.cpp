@@ -8,12 +8,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "lj_gb300.h"
@@ -22,6 +24,42 @@
 #include "lj_schedule.h"
 
 using namespace ljgb;
+
+// ---- allocation hook -------------------------------------------------------
+// g_alloc_budget < 0: allocations go to CUDA.  >= 0: that many more succeed,
+// every later one fails with cudaErrorMemoryAllocation (no CUDA call made)
+// until lj_debug_fail_allocations(-1).
+static std::atomic<long long> g_alloc_budget{-1};
+
+static bool allocation_refused() {
+  long long b = g_alloc_budget.load();
+  while (b >= 0) {
+    if (b == 0) return true;
+    if (g_alloc_budget.compare_exchange_weak(b, b - 1)) return false;
+  }
+  return false;
+}
+
+namespace ljgb {
+
+cudaError_t device_alloc(void** p, size_t bytes) {
+  *p = nullptr;
+  if (allocation_refused()) return cudaErrorMemoryAllocation;
+  return cudaMalloc(p, bytes);
+}
+
+cudaError_t pinned_alloc(void** p, size_t bytes) {
+  *p = nullptr;
+  if (allocation_refused()) return cudaErrorMemoryAllocation;
+  return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
+}  // namespace ljgb
+
+extern "C" lj_status lj_debug_fail_allocations(int64_t after) {
+  g_alloc_budget.store(after < 0 ? -1 : after);
+  return LJ_OK;
+}
 
 namespace {
 
@@ -32,20 +70,49 @@ thread_local std::string g_create_error;
 constexpr int kTileOverhead = 8;
 constexpr int kMaxSegmentsPerBlock = 8;
 
+// Owned device array.  Movable, not copyable; freed on destruction (or
+// explicitly).
+// alloc() replaces the contents: on failure the buffer is left empty.
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      free();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { free(); }
   cudaError_t alloc(size_t count) {
     free();
-    n = count;
     if (count == 0) return cudaSuccess;
-    return cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * count);
+    void* q = nullptr;
+    const cudaError_t e = device_alloc(&q, sizeof(T) * count);
+    if (e != cudaSuccess) return e;
+    p = static_cast<T*>(q);
+    n = count;
+    return cudaSuccess;
   }
   void free() {
     if (p) cudaFree(p);
     p = nullptr;
     n = 0;
+  }
+  void swap(DevBuf& o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
   }
 };
 
@@ -55,11 +122,33 @@ template <typename T>
 struct PinnedBuf {
   T* p = nullptr;
   size_t n = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  PinnedBuf(PinnedBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  PinnedBuf& operator=(PinnedBuf&& o) noexcept {
+    if (this != &o) {
+      free();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~PinnedBuf() { free(); }
   cudaError_t alloc(size_t count) {
     free();
-    n = count;
     if (count == 0) return cudaSuccess;
-    return cudaHostAlloc(reinterpret_cast<void**>(&p), sizeof(T) * count, cudaHostAllocDefault);
+    void* q = nullptr;
+    const cudaError_t e = pinned_alloc(&q, sizeof(T) * count);
+    if (e != cudaSuccess) return e;
+    p = static_cast<T*>(q);
+    n = count;
+    return cudaSuccess;
   }
   void free() {
     if (p) cudaFreeHost(p);
@@ -101,6 +190,8 @@ struct lj_system {
   bool tuned = false;
   Schedule sched;
   int BI = 128;
+  int sched_shape = -1;  // shape and split cap the uploaded schedule was built for
+  int sched_split = 0;
 
   // device memory
   DevBuf<double> x, v, f, tf, e, w;
@@ -300,8 +391,12 @@ lj_status upload_boxes(lj_system* s) {
   return LJ_OK;
 }
 
-// Builds the stream-K schedule for the active shape and uploads its tables.
-lj_status setup_schedule(lj_system* s) {
+// Builds the stream-K schedule for the active shape and split cap and
+// uploads its tables.  All-or-nothing: the new tables are allocated and
+// filled beside the old ones and swapped in only once complete, so a
+// failure (an allocation, say) leaves the handle on its previous schedule,
+// with shape and split cap put back to the ones that schedule was built for.
+lj_status build_and_swap_schedule(lj_system* s) {
   int threads, tile, blocks_per_sm = 0;
   if (s->prec == LJ_PREC_FP64) {
     threads = fp64_block_threads();
@@ -325,40 +420,63 @@ lj_status setup_schedule(lj_system* s) {
   Schedule sch;
   if (!build_schedule(n.data(), s->nsys, threads, tile, G, kTileOverhead, &sch))
     return fail(s, LJ_ERR_INVALID, "cannot build the pair schedule");
+  const int nb = (int)sch.blocks.size();
+  DevBuf<BlockInfo> blocks;
+  DevBuf<int> ctb, clo, cb, cj, sbf, bcnt, gcnt;
+  DevBuf<double> bpart;
+  DevBuf<float> partial;
+  LJ_CUDA(s, blocks.alloc(nb));
+  LJ_CUDA(s, ctb.alloc(sch.G + 1));
+  LJ_CUDA(s, clo.alloc(sch.G + 1));
+  LJ_CUDA(s, cb.alloc(sch.G));
+  LJ_CUDA(s, cj.alloc(sch.G));
+  LJ_CUDA(s, sbf.alloc(s->nsys + 1));
+  LJ_CUDA(s, bpart.alloc((size_t)nb * 8));
+  LJ_CUDA(s, bcnt.alloc(nb));
+  LJ_CUDA(s, gcnt.alloc(4 + (size_t)s->nsys));
+  // partial: nseg x 5 x BI values of 8 bytes (FP64) or 4 bytes (MIXED)
+  const size_t vals = (size_t)sch.nseg * 5 * threads;
+  LJ_CUDA(s, partial.alloc(vals * (s->prec == LJ_PREC_FP64 ? 2 : 1)));
+  LJ_CUDA(s, cudaMemsetAsync(bcnt.p, 0, sizeof(int) * nb, s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(gcnt.p, 0, sizeof(int) * gcnt.n, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(blocks.p, sch.blocks.data(), sizeof(BlockInfo) * nb, cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(ctb.p, sch.cta_tile_begin.data(), sizeof(int) * (sch.G + 1), cudaMemcpyHostToDevice,
+                             s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(clo.p, sch.cta_lo.data(), sizeof(int) * (sch.G + 1), cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(cb.p, sch.cta_block.data(), sizeof(int) * sch.G, cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(cj.p, sch.cta_jt.data(), sizeof(int) * sch.G, cudaMemcpyHostToDevice, s->stream));
+  LJ_CUDA(s, cudaMemcpyAsync(sbf.p, sch.sys_block_first.data(), sizeof(int) * (s->nsys + 1), cudaMemcpyHostToDevice,
+                             s->stream));
+  // also waits for all earlier work on the stream, which may still read the
+  // old tables freed below
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  clear_graphs(s);  // captured graphs name the old tables
+  s->blocks.swap(blocks);
+  s->cta_tile_begin.swap(ctb);
+  s->cta_lo.swap(clo);
+  s->cta_block.swap(cb);
+  s->cta_jt.swap(cj);
+  s->sys_block_first.swap(sbf);
+  s->blk_part.swap(bpart);
+  s->blk_cnt.swap(bcnt);
+  s->glob_cnt.swap(gcnt);
+  s->partial.swap(partial);
   s->sched = std::move(sch);
   s->BI = threads;
   s->hist_shape = -1;  // the histogram pass re-cuts its ranges on next use
-  const int nb = nblocks(s);
-  LJ_CUDA(s, s->blocks.alloc(nb));
-  LJ_CUDA(s, s->cta_tile_begin.alloc(s->sched.G + 1));
-  LJ_CUDA(s, s->cta_lo.alloc(s->sched.G + 1));
-  LJ_CUDA(s, s->cta_block.alloc(s->sched.G));
-  LJ_CUDA(s, s->cta_jt.alloc(s->sched.G));
-  LJ_CUDA(s, s->sys_block_first.alloc(s->nsys + 1));
-  LJ_CUDA(s, s->blk_part.alloc((size_t)nb * 8));
-  LJ_CUDA(s, s->blk_cnt.alloc(nb));
-  LJ_CUDA(s, s->glob_cnt.alloc(4 + (size_t)s->nsys));
-  LJ_CUDA(s, cudaMemsetAsync(s->blk_cnt.p, 0, sizeof(int) * nb, s->stream));
-  LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n, s->stream));
   s->pred_ready = false;
-  // partial: nseg x 5 x BI values of 8 bytes (FP64) or 4 bytes (MIXED)
-  const size_t vals = (size_t)s->sched.nseg * 5 * threads;
-  LJ_CUDA(s, s->partial.alloc(vals * (s->prec == LJ_PREC_FP64 ? 2 : 1)));
-  LJ_CUDA(s, cudaMemcpyAsync(s->blocks.p, s->sched.blocks.data(), sizeof(BlockInfo) * nb, cudaMemcpyHostToDevice,
-                             s->stream));
-  LJ_CUDA(s, cudaMemcpyAsync(s->cta_tile_begin.p, s->sched.cta_tile_begin.data(), sizeof(int) * (s->sched.G + 1),
-                             cudaMemcpyHostToDevice, s->stream));
-  LJ_CUDA(s, cudaMemcpyAsync(s->cta_lo.p, s->sched.cta_lo.data(), sizeof(int) * (s->sched.G + 1),
-                             cudaMemcpyHostToDevice, s->stream));
-  LJ_CUDA(s, cudaMemcpyAsync(s->cta_block.p, s->sched.cta_block.data(), sizeof(int) * s->sched.G,
-                             cudaMemcpyHostToDevice, s->stream));
-  LJ_CUDA(s, cudaMemcpyAsync(s->cta_jt.p, s->sched.cta_jt.data(), sizeof(int) * s->sched.G, cudaMemcpyHostToDevice,
-                             s->stream));
-  LJ_CUDA(s, cudaMemcpyAsync(s->sys_block_first.p, s->sched.sys_block_first.data(), sizeof(int) * (s->nsys + 1),
-                             cudaMemcpyHostToDevice, s->stream));
-  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
-  clear_graphs(s);
+  s->sched_shape = s->shape;
+  s->sched_split = s->split_cap;
   return LJ_OK;
+}
+
+lj_status setup_schedule(lj_system* s) {
+  const lj_status st = build_and_swap_schedule(s);
+  if (st != LJ_OK && s->sched_shape >= 0) {
+    s->shape = s->sched_shape;
+    s->split_cap = s->sched_split;
+  }
+  return st;
 }
 
 // ---- kernel sequences ----------------------------------------------------
@@ -399,21 +517,24 @@ lj_status hist_pass_args(lj_system* s, int shape, const int4* q, const HistArgs&
       return fail(s, LJ_ERR_INVALID, "cannot build the histogram schedule");
     if (sch.BI != s->sched.BI || sch.TILE != s->sched.TILE || sch.blocks.size() != s->sched.blocks.size())
       return fail(s, LJ_ERR_INVALID, "histogram schedule does not match the pair schedule's blocks");
-    s->hsched = std::move(sch);
-    const int G = s->hsched.G;
-    LJ_CUDA(s, s->h_cta_tile_begin.alloc(G + 1));
-    LJ_CUDA(s, s->h_cta_lo.alloc(G + 1));
-    LJ_CUDA(s, s->h_cta_block.alloc(G));
-    LJ_CUDA(s, s->h_cta_jt.alloc(G));
-    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_tile_begin.p, s->hsched.cta_tile_begin.data(), sizeof(int) * (G + 1),
-                               cudaMemcpyHostToDevice, s->stream));
-    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_lo.p, s->hsched.cta_lo.data(), sizeof(int) * (G + 1),
-                               cudaMemcpyHostToDevice, s->stream));
-    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_block.p, s->hsched.cta_block.data(), sizeof(int) * G,
-                               cudaMemcpyHostToDevice, s->stream));
-    LJ_CUDA(s, cudaMemcpyAsync(s->h_cta_jt.p, s->hsched.cta_jt.data(), sizeof(int) * G, cudaMemcpyHostToDevice,
+    // new range tables beside the old ones, swapped in once complete
+    const int G = sch.G;
+    DevBuf<int> ctb, clo, cb, cj;
+    LJ_CUDA(s, ctb.alloc(G + 1));
+    LJ_CUDA(s, clo.alloc(G + 1));
+    LJ_CUDA(s, cb.alloc(G));
+    LJ_CUDA(s, cj.alloc(G));
+    LJ_CUDA(s, cudaMemcpyAsync(ctb.p, sch.cta_tile_begin.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice,
                                s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(clo.p, sch.cta_lo.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(cb.p, sch.cta_block.data(), sizeof(int) * G, cudaMemcpyHostToDevice, s->stream));
+    LJ_CUDA(s, cudaMemcpyAsync(cj.p, sch.cta_jt.data(), sizeof(int) * G, cudaMemcpyHostToDevice, s->stream));
     LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+    s->h_cta_tile_begin.swap(ctb);
+    s->h_cta_lo.swap(clo);
+    s->h_cta_block.swap(cb);
+    s->h_cta_jt.swap(cj);
+    s->hsched = std::move(sch);
     s->hist_shape = shape;
     s->hist_nb = h.nb;
   }
@@ -1134,10 +1255,10 @@ lj_status lj_set_recording(lj_system* s, int32_t cap) {
   if (!s || cap < 0) return LJ_ERR_INVALID;
   DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
-  const DevRecord* old_records = s->records.p;
-  const int old_cap = s->rec_cap;
-  LJ_CUDA(s, s->records.alloc((size_t)cap * s->nsys));
-  s->rec_cap = cap;
+  // The new ring is allocated before the old one is let go: if that fails,
+  // recording goes on as before.
+  DevBuf<DevRecord> ring;
+  LJ_CUDA(s, ring.alloc((size_t)cap * s->nsys));
   std::vector<DevScalars> sc;
   lj_status st = read_scalars(s, sc);
   if (st) return st;
@@ -1145,7 +1266,9 @@ lj_status lj_set_recording(lj_system* s, int32_t cap) {
     d.rec_cap = cap;
     d.rec_count = 0;
   }
-  if (s->records.p != old_records || cap != old_cap) clear_graphs(s);  // records pointer / stride are captured
+  clear_graphs(s);  // records pointer and stride are captured
+  s->records.swap(ring);
+  s->rec_cap = cap;
   return write_scalars(s, sc);
 }
 
@@ -1405,11 +1528,21 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
     bins += c.nalpha;
   }
   s->counter_bins = bins;
-  LJ_CUDA(s, s->dcounters.alloc(s->counters.size()));
-  LJ_CUDA(s, s->counter_ring.alloc((size_t)bins * ring_steps));
-  LJ_CUDA(s, cudaMemcpyAsync(s->dcounters.p, s->counters.data(), sizeof(CounterDev) * s->counters.size(),
-                             cudaMemcpyHostToDevice, s->stream));
-  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  // counting starts only once both buffers exist (counter_cap > 0); on a
+  // failure the handle is left with no counters
+  cudaError_t e = s->dcounters.alloc(s->counters.size());
+  if (e == cudaSuccess) e = s->counter_ring.alloc((size_t)bins * ring_steps);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->dcounters.p, s->counters.data(), sizeof(CounterDev) * s->counters.size(),
+                        cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) {
+    s->counters.clear();
+    s->counter_bins = 0;
+    s->dcounters.free();
+    s->counter_ring.free();
+  }
+  LJ_CUDA(s, e);
   s->counter_cap = ring_steps;
   return LJ_OK;
 }
@@ -1517,22 +1650,17 @@ lj_status lj_render(lj_system* s, int32_t box, int32_t axis, int32_t width, int3
   lj_status st = check_status(s);
   if (st) return st;
   const size_t npix = (size_t)width * height;
-  unsigned long long* key = nullptr;
-  uint8_t* img = nullptr;
-  LJ_CUDA(s, cudaMalloc(&key, sizeof(unsigned long long) * npix));
-  cudaError_t e = cudaMalloc(&img, 4 * npix);
-  if (e == cudaSuccess) {
-    int p0 = 0;
-    for (int k = 0; k < box; ++k) p0 += s->cfg[k].n;
-    e = launch_render(s->x.p, s->npad, p0, s->cfg[box].n, axis, width, height, s->boxes[box].L,
-                      radius * s->cfg[box].sigma, key, img, s->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(rgba, img, 4 * npix, cudaMemcpyDeviceToHost, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    s->launches += 2;
-  }
-  cudaFree(key);
-  if (img) cudaFree(img);
-  LJ_CUDA(s, e);
+  DevBuf<unsigned long long> key;
+  DevBuf<uint8_t> img;
+  LJ_CUDA(s, key.alloc(npix));
+  LJ_CUDA(s, img.alloc(4 * npix));
+  int p0 = 0;
+  for (int k = 0; k < box; ++k) p0 += s->cfg[k].n;
+  LJ_CUDA(s, launch_render(s->x.p, s->npad, p0, s->cfg[box].n, axis, width, height, s->boxes[box].L,
+                           radius * s->cfg[box].sigma, key.p, img.p, s->stream));
+  s->launches += 2;
+  LJ_CUDA(s, cudaMemcpyAsync(rgba, img.p, 4 * npix, cudaMemcpyDeviceToHost, s->stream));
+  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   return LJ_OK;
 }
 
@@ -1555,10 +1683,14 @@ lj_status lj_set_kernel_shape(lj_system* s, int32_t shape) {
   if (s->prec == LJ_PREC_FP64) return LJ_OK;  // one FP64 shape
   DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  const int old_forced = s->forced_shape;
   s->forced_shape = shape;
   s->shape = shape < 0 ? 0 : shape;
   lj_status st = setup_schedule(s);
-  if (st) return st;
+  if (st) {
+    s->forced_shape = old_forced;
+    return st;
+  }
   // The i-block length changed: rebuild shadows and the per-block sums.
   return enqueue_compute_forces(s);
 }
@@ -1568,10 +1700,14 @@ lj_status lj_set_split_cap(lj_system* s, int32_t cap) {
   if (cap < 0 || cap > 1024) return fail(s, LJ_ERR_INVALID, "split cap %d out of range [0, 1024]", cap);
   DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  const int old_forced = s->forced_split;
   s->forced_split = cap;
   s->split_cap = cap > 0 ? cap : kMaxSegmentsPerBlock;
   lj_status st = setup_schedule(s);
-  if (st) return st;
+  if (st) {
+    s->forced_split = old_forced;
+    return st;
+  }
   // The partial segments were re-cut: rebuild the per-block sums.
   return enqueue_compute_forces(s);
 }
@@ -1637,10 +1773,34 @@ lj_status lj_autotune(lj_system* s) {
     s->qpar = qpar;
     return LJ_OK;
   };
+  // On a failure part-way (an allocation of a trial schedule, say), the
+  // handle goes back to its own shape and split cap where it can, and to the
+  // snapshotted state, before the error is returned.
+  const int orig_shape = s->shape, orig_split = s->split_cap;
+  auto give_up = [&](lj_status err) -> lj_status {
+    const std::string msg = s->err;
+    s->profiling = was_profiling;
+    s->shape = orig_shape;
+    s->split_cap = orig_split;
+    if (s->sched_shape != orig_shape || s->sched_split != orig_split) setup_schedule(s);
+    if (restore() == LJ_OK && enqueue_compute_forces(s) == LJ_OK &&
+        cudaMemcpyAsync(s->sc.p, snap_sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToDevice, s->stream) ==
+            cudaSuccess)
+      cudaStreamSynchronize(s->stream);
+    s->err = msg;
+    return err;
+  };
   double dt = s->boxes[0].dt > 0 ? s->boxes[0].dt : 0.005;
-  cudaEvent_t e0, e1;
-  LJ_CUDA(s, cudaEventCreate(&e0));
-  LJ_CUDA(s, cudaEventCreate(&e1));
+  struct Events {  // destroyed on every return path
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Events() {
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+  } ev;
+  LJ_CUDA(s, cudaEventCreate(&ev.e0));
+  LJ_CUDA(s, cudaEventCreate(&ev.e1));
+  cudaEvent_t e0 = ev.e0, e1 = ev.e1;
   // Two dimensions: the CTA shape (threads, j-tile, stages) and the threads
   // per particle (the split cap: CTAs an i-block may be cut into).  A cap
   // only matters while it keeps the grid below SMs x resident CTAs; larger
@@ -1654,20 +1814,20 @@ lj_status lj_autotune(lj_system* s) {
       if (s->forced_split > 0 && cap != kSplitCaps[0]) break;
       s->shape = k;
       s->split_cap = s->forced_split > 0 ? s->forced_split : cap;
-      if ((st = setup_schedule(s))) return st;
+      if ((st = setup_schedule(s))) return give_up(st);
       if (s->sched.G == prev_G) break;
       prev_G = s->sched.G;
-      if ((st = restore())) return st;
-      if ((st = enqueue_compute_forces(s))) return st;
-      if ((st = lj_step(s, dt, 2))) return st;
+      if ((st = restore())) return give_up(st);
+      if ((st = enqueue_compute_forces(s))) return give_up(st);
+      if ((st = lj_step(s, dt, 2))) return give_up(st);
       LJ_CUDA(s, cudaEventRecord(e0, s->stream));
       const int reps = 6;
-      if ((st = lj_step(s, dt, reps))) return st;
+      if ((st = lj_step(s, dt, reps))) return give_up(st);
       LJ_CUDA(s, cudaEventRecord(e1, s->stream));
       LJ_CUDA(s, cudaEventSynchronize(e1));
       float ms = 0;
       LJ_CUDA(s, cudaEventElapsedTime(&ms, e0, e1));
-      if ((st = check_status(s))) return st;
+      if ((st = check_status(s))) return give_up(st);
       if (ms < best_ms) {
         best_ms = ms;
         best = k;
@@ -1675,13 +1835,11 @@ lj_status lj_autotune(lj_system* s) {
       }
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   s->shape = best;
   s->split_cap = best_split;
-  s->tuned = true;
   s->profiling = was_profiling;
-  if ((st = setup_schedule(s))) return st;
+  if ((st = setup_schedule(s))) return give_up(st);
+  s->tuned = true;
   if ((st = restore())) return st;
   // The restored shadow and sums belong to the old i-block length: rebuild
   // forces, then put back the observables and running sums.
@@ -1774,7 +1932,7 @@ const char* lj_version(void) { return "lj_gb300 1.0 (sm_103a)"; }
 
 void* lj_host_alloc(size_t bytes) {
   void* p = nullptr;
-  if (bytes == 0 || cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  if (bytes == 0 || pinned_alloc(&p, bytes) != cudaSuccess) return nullptr;
   return p;
 }
 

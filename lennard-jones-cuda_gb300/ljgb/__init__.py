@@ -89,6 +89,7 @@ def _declare(L):
         "lj_set_recording": (C.c_int, [_P, C.c_int32]),
         "lj_get_records": (C.c_int, [_P, C.POINTER(Observables), C.c_int32, C.POINTER(C.c_int32)]),
         "lj_batch_records": (C.c_int, [_P, C.c_int32, C.POINTER(Observables), C.c_int32, C.POINTER(C.c_int32)]),
+        "lj_debug_fail_allocations": (C.c_int, [C.c_int64]),
         "lj_reset_averaging": (C.c_int, [_P]),
         "lj_set_canonical": (C.c_int, [_P, C.c_int32]),
         "lj_set_boundary": (C.c_int, [_P, C.c_int32]),

@@ -156,6 +156,32 @@ def test_static_rejects_a_capturing_stream(ljlib):
     ljlib.deleteArray(d_frc)
 
 
+def test_static_works_while_every_allocation_fails(ljlib):
+    """With the library's allocation hook refusing every device and host
+    allocation (lj_debug_fail_allocations(0)), the entry point still works:
+    it allocates nothing."""
+    fn = bind(ljlib)
+    n = 1500
+    pos, _, L = U.lattice_state(n, 0.8, 1.0, "fcc", 0.02, seed=21)
+    pos4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = pos
+    d_pos, d_frc = device_array(ljlib, n), device_array(ljlib, n)
+    ljlib.copyArrayToDevice(d_pos, pos4.ctypes.data, n)
+    f_ref, pressure = run_existing(ljlib, d_pos, n, np.float32(L), True)
+    ljlib.lj_debug_fail_allocations(0)
+    try:
+        for _ in range(2):
+            sums = np.zeros(2)
+            assert fn(d_pos, d_frc, sums.ctypes.data, n, C.c_float(L), 1, None) == 0
+    finally:
+        ljlib.lj_debug_fail_allocations(-1)
+    f = np.zeros((n, 4), np.float32)
+    ljlib.copyArrayFromDevice(f.ctypes.data, d_frc, 0, n)
+    compare(f, f_ref, sums, pressure)
+    ljlib.deleteArray(d_pos)
+    ljlib.deleteArray(d_frc)
+
+
 def test_static_rejects_oversized_box(ljlib):
     fn = bind(ljlib)
     d = device_array(ljlib, 4)
