@@ -134,6 +134,17 @@ lj_status lj_reinitialize(lj_system* sys, const lj_config* cfg);
  * Forces are NOT recomputed; call lj_compute_forces. */
 lj_status lj_set_state(lj_system* sys, const double* pos, const double* vel);
 
+/* lj_set_state without its synchronisation: the upload, its finiteness check
+ * and the unpack are queued on the handle's stream and the call returns.
+ * For a host loop that uploads, steps and reads back every step
+ * (lj_set_state_async + lj_step + lj_get_state_observables: one host
+ * synchronisation per step).  The caller keeps pos / vel unchanged until the
+ * next synchronising call (lj_sync, lj_get_*) returns.  A non-finite value
+ * drops the upload on the device (the state stays as it was, and later
+ * queued uploads are dropped too) and is reported as LJ_ERR_INVALID by that
+ * next synchronising call.  No counterpart in the reference. */
+lj_status lj_set_state_async(lj_system* sys, const double* pos, const double* vel);
+
 /* Read back state (N x 3 doubles each, any may be NULL) -- getArray(0/1)
  * (MDSystem.cpp:586-613) and h_Force. */
 lj_status lj_get_state(lj_system* sys, double* pos, double* vel, double* force);

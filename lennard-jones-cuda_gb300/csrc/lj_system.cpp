@@ -198,6 +198,7 @@ struct lj_system {
   DevBuf<double> stage;          // 3 x (N,3) interleaved host-format arrays: positions, velocities, forces
   DevBuf<int> bad;               // lowest index of a non-finite uploaded value (INT_MAX: none)
   PinnedBuf<int> h_words;        // [0] status, [1] bad index: read back after one synchronisation
+  bool upload_check_pending = false;  // lj_set_state_async queued a finiteness check not yet read back
   PinnedBuf<DevScalars> h_sc;    // per-box scalars read back
   DevBuf<int4> q, q2;  // fixed-point shadow, double-buffered for the fused step
   DevBuf<double4_32a> xd;
@@ -750,7 +751,14 @@ lj_status after_step(lj_system* s) {
 // back by a copy enqueued behind the work (one synchronisation in all).
 lj_status sync_status(lj_system* s) {
   LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  const bool upload = s->upload_check_pending;
+  if (upload)
+    LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p + 1, s->bad.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->upload_check_pending = false;
+  if (upload && s->h_words.p[1] != 0x7f7f7f7f)
+    return fail(s, LJ_ERR_INVALID, "an array queued by lj_set_state_async held a non-finite value (element %d of "
+                "the staged upload); it was dropped and the state left as it was", s->h_words.p[1]);
   const int st = s->h_words.p[0];
   if (st) {
     // (on the handle's stream: it is non-blocking, so a legacy-stream memset
@@ -1069,17 +1077,16 @@ lj_status lj_reinitialize(lj_system* s, const lj_config* cfg) {
 // the device; the state is written only if every value is finite, so a
 // rejected call leaves it unchanged.  One synchronisation (the caller's
 // buffers are free on return).
-lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
-  if (!s) return LJ_ERR_INVALID;
-  if (!pos && !vel) return LJ_OK;
-  DeviceGuard device_guard(s->device);
-  lj_status fst = flush_observables(s);
-  if (fst) return fst;
+// Queues the upload of pos / vel through the staging buffer: copies, the
+// finiteness check (lowest bad index into s->bad) and the checked unpack.
+// A check still pending from an earlier queued upload keeps its index, so a
+// rejection is never lost (later uploads are then dropped too).
+static lj_status enqueue_upload(lj_system* s, const double* pos, const double* vel) {
   s->pred_ready = false;
   const size_t n3 = 3 * (size_t)s->ntotal;
   double* st_pos = s->stage.p;
   double* st_vel = s->stage.p + n3;
-  LJ_CUDA(s, cudaMemsetAsync(s->bad.p, 0x7f, sizeof(int), s->stream));
+  if (!s->upload_check_pending) LJ_CUDA(s, cudaMemsetAsync(s->bad.p, 0x7f, sizeof(int), s->stream));
   if (pos) LJ_CUDA(s, cudaMemcpyAsync(st_pos, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
   if (vel) LJ_CUDA(s, cudaMemcpyAsync(st_vel, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
   LJ_CUDA(s, launch_check_finite(pos ? st_pos : st_vel, (pos && vel) ? 2 * n3 : n3, s->bad.p, s->stream));
@@ -1095,6 +1102,19 @@ lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
   }
   LJ_CUDA(s, launch_unpack_multi_checked(xa, na, s->ntotal, s->npad, s->bad.p, s->stream));
   s->launches += 2;
+  return LJ_OK;
+}
+
+lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
+  if (!s) return LJ_ERR_INVALID;
+  if (!pos && !vel) return LJ_OK;
+  DeviceGuard device_guard(s->device);
+  lj_status fst = flush_observables(s);
+  if (fst) return fst;
+  // a rejection still pending from lj_set_state_async is reported first
+  if (s->upload_check_pending && (fst = sync_status(s))) return fst;
+  const size_t n3 = 3 * (size_t)s->ntotal;
+  if ((fst = enqueue_upload(s, pos, vel))) return fst;
   LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p + 1, s->bad.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   const int bad = s->h_words.p[1];
@@ -1105,6 +1125,20 @@ lj_status lj_set_state(lj_system* s, const double* pos, const double* vel) {
   }
   // A walled box keeps its fixed-point frame between steps: rebuild it
   // around the new positions.
+  if (pos && s->any_nonperiodic) return enqueue_frame_all(s);
+  return LJ_OK;
+}
+
+lj_status lj_set_state_async(lj_system* s, const double* pos, const double* vel) {
+  if (!s) return LJ_ERR_INVALID;
+  if (!pos && !vel) return LJ_OK;
+  DeviceGuard device_guard(s->device);
+  lj_status st = flush_observables(s);
+  if (st) return st;
+  if ((st = enqueue_upload(s, pos, vel))) return st;
+  s->upload_check_pending = true;
+  // A walled box keeps its fixed-point frame between steps: rebuild it
+  // around the new positions (around the old ones if the upload is dropped).
   if (pos && s->any_nonperiodic) return enqueue_frame_all(s);
   return LJ_OK;
 }

@@ -77,6 +77,7 @@ def _declare(L):
         "lj_get_info": (C.c_int, [_P, C.POINTER(C.c_int32), _dp]),
         "lj_reinitialize": (C.c_int, [_P, C.POINTER(Config)]),
         "lj_set_state": (C.c_int, [_P, _P, _P]),
+        "lj_set_state_async": (C.c_int, [_P, _P, _P]),
         "lj_get_state": (C.c_int, [_P, _P, _P, _P]),
         "lj_get_pair_sums": (C.c_int, [_P, _P, _P]),
         "lj_compute_forces": (C.c_int, [_P]),
@@ -345,6 +346,12 @@ class System:
     def set_state_from(self, pos=None, vel=None):
         ptr = lambda a: a.ctypes.data if a is not None else None
         self._c(load().lj_set_state(self.h, ptr(pos), ptr(vel)))
+
+    def set_state_async_from(self, pos=None, vel=None):
+        """lj_set_state_async: queued upload; pos / vel must stay unchanged
+        (and alive) until the next synchronising call returns."""
+        ptr = lambda a: a.ctypes.data if a is not None else None
+        self._c(load().lj_set_state_async(self.h, ptr(pos), ptr(vel)))
 
     def pair_sums(self):
         e = np.zeros(self.ntotal)

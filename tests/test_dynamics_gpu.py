@@ -291,6 +291,45 @@ def test_set_state_checks_and_round_trips(ljgb_mod):
     assert s.observables()["step"] == 5
 
 
+@pytest.mark.parametrize("boundary", [0, 1])
+def test_set_state_async(ljgb_mod, boundary):
+    """lj_set_state_async queues what lj_set_state does: an upload/step/read
+    loop with one synchronisation per step gives the same trajectory, bit for
+    bit, as the synchronous uploads; a non-finite upload is dropped on the
+    device and reported by the next synchronising call."""
+    kw = dict(n=900, density=0.7, temperature=1.1, canonical=1, boundary=boundary,
+              lattice=ljgb_mod.LATTICE_FCC, jitter=0.02, seed=4)
+    a, b = ljgb_mod.System(**kw), ljgb_mod.System(**kw)
+    pa, va = ljgb_mod.pinned((900, 3)), ljgb_mod.pinned((900, 3))
+    pb, vb = ljgb_mod.pinned((900, 3)), ljgb_mod.pinned((900, 3))
+    a.get_state_into(pa, va, None)
+    b.get_state_into(pb, vb, None)
+    for _ in range(6):
+        va *= 0.999                      # the host changes the state between steps
+        vb *= 0.999
+        a.set_state_async_from(pa, va)
+        b.set_state_from(pb, vb)
+        a.integrate(0.005)
+        b.integrate(0.005)
+        oa = a.get_state_observables_into(pa, va, None)
+        ob = b.get_state_observables_into(pb, vb, None)
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+        assert oa["U"] == ob["U"] and oa["step"] == ob["step"]
+    p0, v0, f0 = a.get_state()
+    bad = ljgb_mod.pinned((900, 3))
+    bad[:] = v0
+    bad[17, 0] = np.nan
+    a.set_state_async_from(None, bad)    # queued; the check runs on the device
+    with pytest.raises(ljgb_mod.LJError, match="lj_set_state_async"):
+        a.sync()
+    p1, v1, f1 = a.get_state()
+    assert np.array_equal(p1, p0) and np.array_equal(v1, v0) and np.array_equal(f1, f0)
+    a.integrate(0.005, 2)
+    assert np.isfinite(a.observables()["U"])
+    a.close()
+    b.close()
+
+
 def test_walls_frame_follows_set_state(ljgb_mod):
     """A walled box's fixed frame is rebuilt around positions set from the
     host, even far outside the walls; the wall turns the particle back."""
