@@ -28,6 +28,14 @@ namespace ljgb {
 // Cost: one FP64 multiply, one conversion and a few integer operations (FP64
 // runs at 1/64 of the FP32 rate on this part).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t fixed_coord_scaled(double dx, double scale) {
+  const double t = dx * scale;
+  const uint32_t u = (uint32_t)(unsigned long long)llrint(t);
+  const uint32_t r = u % 3u;
+  const uint32_t q = r == 0u ? u : (r == 1u ? u - 1u : u + 1u);
+  return (int32_t)q;
+}
+
 __device__ __forceinline__ int32_t fixed_coord(double x, double origin, double invP) {
   const double t = (x - origin) * (invP * 4294967296.0);
   const uint32_t u = (uint32_t)(unsigned long long)llrint(t);

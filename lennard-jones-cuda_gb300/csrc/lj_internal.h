@@ -113,6 +113,7 @@ struct BoxArgs {
   // the step kernels multiply instead of divide (FP64 division is a long
   // dependent sequence on this part's narrow FP64 pipe).
   double hdt;    // dt / 2
+  double qdt;    // dt / 4: the TVN kick dt/2 of the averaged force (F_n + F_{n+1}) / 2
   double hdt2;   // dt^2 / 2
   double eps4;   // 4 eps
   double kT;     // 2 / (3 N):  T = kT K

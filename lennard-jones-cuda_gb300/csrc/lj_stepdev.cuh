@@ -11,15 +11,29 @@
 
 namespace ljgb {
 
+// Sign and order tests of FP64 values on their bit patterns (integer pipe;
+// the FP64 pipe issues at 1/64 of the FP32 rate on this part).  For x not
+// NaN: x < 0 exactly when the bits are negative as a signed integer and not
+// those of -0.0; x > L (L > 0) exactly when the bits are larger than L's.
+// For NaN both forms leave NaN behind, so results agree bit for bit.
+__device__ __forceinline__ bool neg_bits(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && b != (long long)0x8000000000000000ull;
+}
+__device__ __forceinline__ bool above_bits(double x, long long Lbits) { return __double_as_longlong(x) > Lbits; }
+
 // ApplyBoundaryConditions (MDSystem.cpp:406-436) for one coordinate: wrap
 // (periodic) or reflect the velocity (walls); open boxes leave both alone.
 __device__ __forceinline__ void apply_bc1(int bc, double L, double& x, double& v) {
+  const long long Lbits = __double_as_longlong(L);
   if (bc == 0) {
-    if (x < 0.) x += L;
-    if (x > L) x -= L;
+    if (neg_bits(x)) x += L;
+    if (above_bits(x, Lbits)) x -= L;
   } else if (bc == 1) {
-    if (x < 0. && v < 0) v = -v;
-    if (x > L && v > 0) v = -v;
+    // v = -v is a flip of the sign bit
+    if (neg_bits(x) && neg_bits(v)) v = __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+    if (above_bits(x, Lbits) && __double_as_longlong(v) > 0)
+      v = __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
   }
 }
 
@@ -62,6 +76,16 @@ __device__ __forceinline__ void check_wall_frame(const StateArgs& s, int bc, con
 __device__ __forceinline__ int4 shadow_of(const DevScalars& sc, double x, double y, double z) {
   return make_int4(fixed_coord(x, sc.origin[0], sc.invP), fixed_coord(y, sc.origin[1], sc.invP),
                    fixed_coord(z, sc.origin[2], sc.invP), 0);
+}
+
+// shadow_of for a box of boundary bc with the frame scale formed once; a
+// periodic box's frame has origin 0, so its subtraction is skipped (x - 0 is
+// x exactly): the same bits as shadow_of.
+__device__ __forceinline__ int4 shadow_of_bc(const DevScalars& sc, int bc, double x, double y, double z) {
+  const double scale = sc.invP * 4294967296.0;
+  if (bc == 0) return make_int4(fixed_coord_scaled(x, scale), fixed_coord_scaled(y, scale), fixed_coord_scaled(z, scale), 0);
+  return make_int4(fixed_coord_scaled(x - sc.origin[0], scale), fixed_coord_scaled(y - sc.origin[1], scale),
+                   fixed_coord_scaled(z - sc.origin[2], scale), 0);
 }
 
 // Sum of blk_part[b][slot] over the blocks of one box, fixed order, valid in
@@ -252,18 +276,19 @@ __device__ __noinline__ void fused_block_step(const StateArgs& s, int B, double*
         vv = fma(v, v, vv);
       }
       check_wall_frame(s, box.bc, sc, xp[0], xp[1], xp[2]);
-      s.q_next[p] = shadow_of(sc, xp[0], xp[1], xp[2]);
-      part[0] = 0.5 * vv;
-      part[1] = 0.5 * e;
+      s.q_next[p] = shadow_of_bc(sc, box.bc, xp[0], xp[1], xp[2]);
+      part[0] = vv;  // K and V shares, halved once per block below
+      part[1] = e;
       part[2] = w;
     } else {
       double tv2 = 0.0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const size_t k = (size_t)c * s.npad + p;
-        const double tf = 0.5 * s.f[k] + 0.5 * Fn1[c];  // as k_tvn_close forms it
+        // v + dt/2 (F_n + F_{n+1})/2 as v + dt/4 (F_n + F_{n+1}): the same
+        // bits (the halvings are exact), one FP64 operation fewer
+        const double tv = fma(box.qdt, s.f[k] + Fn1[c], s.v[k]);
         s.tf[k] = Fn1[c];
-        const double tv = fma(box.hdt, tf, s.v[k]);
         tv2 = fma(tv, tv, tv2);
       }
       part[0] = tv2;
@@ -272,8 +297,10 @@ __device__ __noinline__ void fused_block_step(const StateArgs& s, int B, double*
   block_sum<NP>(part, sh);
   if (tid == 0) {
     if constexpr (MODE == MODE_EVN) {
-#pragma unroll
-      for (int c = 0; c < NP; ++c) s.blk_part[(size_t)B * 8 + s.obs_slot + c] = part[c];
+      // halving the block sums gives the bits of summing halved terms
+      s.blk_part[(size_t)B * 8 + s.obs_slot + 0] = 0.5 * part[0];
+      s.blk_part[(size_t)B * 8 + s.obs_slot + 1] = 0.5 * part[1];
+      s.blk_part[(size_t)B * 8 + s.obs_slot + 2] = part[2];
     } else {
       s.blk_part[(size_t)B * 8 + 3] = part[0];
     }

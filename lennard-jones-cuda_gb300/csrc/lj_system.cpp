@@ -378,6 +378,7 @@ lj_status upload_boxes(lj_system* s) {
   for (auto& b : s->boxes) {
     s->any_nonperiodic |= (b.bc != 0);
     b.hdt = 0.5 * b.dt;
+    b.qdt = 0.25 * b.dt;
     b.hdt2 = 0.5 * b.dt * b.dt;
     b.eps4 = 4.0 * b.eps;
     b.kT = 2.0 / (3.0 * b.N);
