@@ -210,24 +210,23 @@ def timed_steps(torch, s, steps, warmup, flush, dt=DT):
 
 
 def e2e_steps(ljgb, s, steps, warmup):
-    """Through the public API with host buffers: per step upload pos+vel from
-    pinned memory (lj_set_state_async, queued), one step (lj_step), download
-    pos+vel and the observables (lj_get_state_observables, which synchronises
-    once and reports the upload's finiteness check)."""
+    """Through the public API with host buffers: every step is one lj_step_io
+    call -- upload of pos+vel from page-locked host memory (queued; the
+    kernels read it over NVLink-C2C), one step, read-back of pos+vel (written
+    by the pack kernel into host memory) and of the observables, one host
+    synchronisation, which also reports the upload's finiteness check."""
     pos = ljgb.pinned((N, 3))
     vel = ljgb.pinned((N, 3))
     s.get_state_into(pos, vel, None)
     for _ in range(warmup):
-        s.set_state_async_from(pos, vel)
-        s.integrate(DT)
-        s.get_state_observables_into(pos, vel, None)
+        s.step_io(DT, 1, pos, vel, pos, vel)
     t0 = time.perf_counter()
     for _ in range(steps):
-        s.set_state_async_from(pos, vel)
-        s.integrate(DT)
-        s.get_state_observables_into(pos, vel, None)
+        s.step_io(DT, 1, pos, vel, pos, vel)
     el = time.perf_counter() - t0
-    obs_bytes = 208 + 4  # the box's device scalar block (observables, clock, averages) and the status word
+    # the box's device scalar block (208 B: observables, clock, averages), the
+    # status word and the upload check's result
+    obs_bytes = 208 + 4 + 4
     return el, {"h2d_bytes_per_step": 2 * N * 3 * 8, "d2h_bytes_per_step": 2 * N * 3 * 8 + obs_bytes}
 
 

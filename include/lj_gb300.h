@@ -145,6 +145,17 @@ lj_status lj_set_state(lj_system* sys, const double* pos, const double* vel);
  * next synchronising call.  No counterpart in the reference. */
 lj_status lj_set_state_async(lj_system* sys, const double* pos, const double* vel);
 
+/* One host round trip for a caller that keeps the state on the host (the
+ * reference's host loop: write h_Pos/h_Vel, Integrate(dt), read them back,
+ * MDSystem.cpp:438-583, 586-630): lj_set_state_async(pos_in, vel_in), then
+ * lj_step(dt, nsteps), then lj_get_state_observables(pos_out, vel_out,
+ * force_out, obs) -- one host synchronisation.  Any array may be NULL;
+ * outputs may be the input buffers.  Page-locked host buffers (lj_host_alloc)
+ * are read and written by the kernels directly, others through staged
+ * copies.  No counterpart in the reference. */
+lj_status lj_step_io(lj_system* sys, const double* pos_in, const double* vel_in, double dt, int32_t nsteps,
+                     double* pos_out, double* vel_out, double* force_out, lj_observables* obs);
+
 /* Read back state (N x 3 doubles each, any may be NULL) -- getArray(0/1)
  * (MDSystem.cpp:586-613) and h_Force. */
 lj_status lj_get_state(lj_system* sys, double* pos, double* vel, double* force);

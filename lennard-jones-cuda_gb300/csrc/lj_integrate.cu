@@ -538,8 +538,20 @@ __global__ void k_unpack(const double* __restrict__ in, double* __restrict__ out
 }
 
 // Up to three (N,3) <-> component-major transposes in one launch; blockIdx.y
-// selects the array.
-__global__ void k_pack_multi(XyzArrays a, int n, int npad) {
+// selects the array.  With a mailbox, the row after the arrays copies the
+// status words and the scalar block into the handle's page-locked mirrors
+// (destinations may be mapped host memory: the host reads them after one
+// synchronisation, with no copy operation queued).
+__global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb) {
+  if ((int)blockIdx.y == count) {
+    if (blockIdx.x != 0) return;
+    if (threadIdx.x == 0) {
+      mb.words_out[0] = *mb.status;
+      if (mb.bad) mb.words_out[1] = *mb.bad;
+    }
+    for (int k = threadIdx.x; k < mb.sc_nwords; k += blockDim.x) mb.sc_out[k] = mb.sc[k];
+    return;
+  }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* __restrict__ in = a.src[blockIdx.y];
@@ -560,11 +572,17 @@ __global__ void k_unpack_multi_checked(XyzArrays a, int n, int npad, const int* 
   for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
 }
 
-// Lowest index of a non-finite value among `count` staged values (bad starts
-// at 0x7f7f7f7f).
-__global__ void k_check_finite(const double* __restrict__ in, long long count, int* bad) {
+// Lowest index of a non-finite value among the na values of a followed by
+// the nb values of b (bad starts at 0x7f7f7f7f); blockIdx.y selects the
+// array.  Either may be host memory mapped into the device's address space.
+__global__ void k_check_finite2(const double* __restrict__ a, long long na, const double* __restrict__ b,
+                                long long nb, int* bad) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < count && !isfinite(in[i])) atomicMin(bad, (int)i);
+  if (blockIdx.y == 0) {
+    if (i < na && !isfinite(a[i])) atomicMin(bad, (int)i);
+  } else if (i < nb && !isfinite(b[i])) {
+    atomicMin(bad, (int)(na + i));
+  }
 }
 
 // A wait that nothing completes: the pair kernels' bounded mbarrier wait must
@@ -590,9 +608,10 @@ cudaError_t launch_selftest_wait(int* status, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_check_finite(const double* in, size_t count, int* bad, cudaStream_t st) {
-  if (count == 0) return cudaSuccess;
-  k_check_finite<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, (long long)count, bad);
+cudaError_t launch_check_finite2(const double* a, size_t na, const double* b, size_t nb, int* bad, cudaStream_t st) {
+  const size_t m = na > nb ? na : nb;
+  if (m == 0) return cudaSuccess;
+  k_check_finite2<<<dim3((unsigned)((m + 255) / 256), 2), 256, 0, st>>>(a, (long long)na, b, (long long)nb, bad);
   return cudaGetLastError();
 }
 
@@ -601,9 +620,10 @@ cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaSt
   return cudaGetLastError();
 }
 
-cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, cudaStream_t st) {
-  if (count <= 0) return cudaSuccess;
-  k_pack_multi<<<dim3((n + 255) / 256, count), 256, 0, st>>>(a, n, npad);
+cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, cudaStream_t st) {
+  const int rows = count + (mb ? 1 : 0);
+  if (rows <= 0) return cudaSuccess;
+  k_pack_multi<<<dim3((n + 255) / 256, rows), 256, 0, st>>>(a, count, n, npad, mb ? *mb : Mailbox{});
   return cudaGetLastError();
 }
 

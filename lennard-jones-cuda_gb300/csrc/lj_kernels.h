@@ -149,13 +149,26 @@ cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, in
                             cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_selftest_wait(int* status, cudaStream_t st);
-cudaError_t launch_check_finite(const double* in, size_t count, int* bad, cudaStream_t st);
+// Lowest index of a non-finite value in a[0..na) then b[0..nb) (index na + k
+// for b[k]); either array may be mapped host memory.
+cudaError_t launch_check_finite2(const double* a, size_t na, const double* b, size_t nb, int* bad, cudaStream_t st);
 // Up to three (N,3) interleaved <-> component-major [3][npad] transposes in one launch.
 struct XyzArrays {
   const double* src[3];
   double* dst[3];
 };
-cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, cudaStream_t st);
+// Small device words copied by the pack launch: the status word (and the
+// upload check's bad index, if bad is set) to words_out[0..1], and
+// sc_nwords 32-bit words of the scalar block to sc_out.
+struct Mailbox {
+  const int* status;
+  const int* bad;
+  int* words_out;
+  const int* sc;
+  int* sc_out;
+  int sc_nwords;
+};
+cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, cudaStream_t st);
 cudaError_t launch_unpack_multi_checked(const XyzArrays& a, int count, int n, int npad, const int* bad,
                                         cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,

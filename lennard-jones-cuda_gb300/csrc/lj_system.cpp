@@ -122,20 +122,24 @@ template <typename T>
 struct PinnedBuf {
   T* p = nullptr;
   size_t n = 0;
+  void* dev = nullptr;  // the same memory's device address (mapped), nullptr if it has none
   PinnedBuf() = default;
   PinnedBuf(const PinnedBuf&) = delete;
   PinnedBuf& operator=(const PinnedBuf&) = delete;
-  PinnedBuf(PinnedBuf&& o) noexcept : p(o.p), n(o.n) {
+  PinnedBuf(PinnedBuf&& o) noexcept : p(o.p), n(o.n), dev(o.dev) {
     o.p = nullptr;
     o.n = 0;
+    o.dev = nullptr;
   }
   PinnedBuf& operator=(PinnedBuf&& o) noexcept {
     if (this != &o) {
       free();
       p = o.p;
       n = o.n;
+      dev = o.dev;
       o.p = nullptr;
       o.n = 0;
+      o.dev = nullptr;
     }
     return *this;
   }
@@ -148,14 +152,34 @@ struct PinnedBuf {
     if (e != cudaSuccess) return e;
     p = static_cast<T*>(q);
     n = count;
+    if (cudaHostGetDevicePointer(&dev, q, 0) != cudaSuccess) {
+      dev = nullptr;
+      (void)cudaGetLastError();
+    }
     return cudaSuccess;
   }
   void free() {
     if (p) cudaFreeHost(p);
     p = nullptr;
     n = 0;
+    dev = nullptr;
   }
 };
+
+// The device address of a caller's host buffer when it is page-locked and
+// mapped into the current device's address space (lj_host_alloc memory,
+// other page-locked allocations): kernels then read or write it directly
+// (over NVLink-C2C on Grace) instead of a staged copy.  nullptr otherwise
+// (pageable memory takes the staged path).
+void* mapped_device_ptr(const void* host) {
+  if (!host) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
 
 struct GraphEntry {
   cudaGraph_t graph = nullptr;  // kept: exec-graph node updates name nodes of this graph
@@ -750,11 +774,19 @@ lj_status after_step(lj_system* s) {
 
 // Waits for the handle's stream and reports the device status word, read
 // back by a copy enqueued behind the work (one synchronisation in all).
-lj_status sync_status(lj_system* s) {
+// Queues the copies of the status word (and a pending upload check's bad
+// index) into h_words.
+lj_status enqueue_status_read(lj_system* s) {
   LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-  const bool upload = s->upload_check_pending;
-  if (upload)
+  if (s->upload_check_pending)
     LJ_CUDA(s, cudaMemcpyAsync(s->h_words.p + 1, s->bad.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  return LJ_OK;
+}
+
+// Synchronises the handle's stream and reports what the status words queued
+// for h_words say.
+lj_status finish_status(lj_system* s) {
+  const bool upload = s->upload_check_pending;
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->upload_check_pending = false;
   if (upload && s->h_words.p[1] != 0x7f7f7f7f)
@@ -779,6 +811,12 @@ lj_status sync_status(lj_system* s) {
                   "positions it started from (blow-up)");
   }
   return LJ_OK;
+}
+
+lj_status sync_status(lj_system* s) {
+  lj_status st = enqueue_status_read(s);
+  if (st) return st;
+  return finish_status(s);
 }
 
 lj_status check_status(lj_system* s) {
@@ -1082,23 +1120,31 @@ lj_status lj_reinitialize(lj_system* s, const lj_config* cfg) {
 // finiteness check (lowest bad index into s->bad) and the checked unpack.
 // A check still pending from an earlier queued upload keeps its index, so a
 // rejection is never lost (later uploads are then dropped too).
+// Page-locked mapped caller buffers are read by the kernels directly; others
+// are copied to the staging buffer first.
 static lj_status enqueue_upload(lj_system* s, const double* pos, const double* vel) {
   s->pred_ready = false;
   const size_t n3 = 3 * (size_t)s->ntotal;
-  double* st_pos = s->stage.p;
-  double* st_vel = s->stage.p + n3;
+  const double* src_pos = static_cast<const double*>(mapped_device_ptr(pos));
+  const double* src_vel = static_cast<const double*>(mapped_device_ptr(vel));
   if (!s->upload_check_pending) LJ_CUDA(s, cudaMemsetAsync(s->bad.p, 0x7f, sizeof(int), s->stream));
-  if (pos) LJ_CUDA(s, cudaMemcpyAsync(st_pos, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
-  if (vel) LJ_CUDA(s, cudaMemcpyAsync(st_vel, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
-  LJ_CUDA(s, launch_check_finite(pos ? st_pos : st_vel, (pos && vel) ? 2 * n3 : n3, s->bad.p, s->stream));
+  if (pos && !src_pos) {
+    LJ_CUDA(s, cudaMemcpyAsync(s->stage.p, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
+    src_pos = s->stage.p;
+  }
+  if (vel && !src_vel) {
+    LJ_CUDA(s, cudaMemcpyAsync(s->stage.p + n3, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
+    src_vel = s->stage.p + n3;
+  }
+  LJ_CUDA(s, launch_check_finite2(src_pos, pos ? n3 : 0, src_vel, vel ? n3 : 0, s->bad.p, s->stream));
   XyzArrays xa{};
   int na = 0;
   if (pos) {
-    xa.src[na] = st_pos;
+    xa.src[na] = src_pos;
     xa.dst[na++] = s->x.p;
   }
   if (vel) {
-    xa.src[na] = st_vel;
+    xa.src[na] = src_vel;
     xa.dst[na++] = s->v.p;
   }
   LJ_CUDA(s, launch_unpack_multi_checked(xa, na, s->ntotal, s->npad, s->bad.p, s->stream));
@@ -1144,9 +1190,12 @@ lj_status lj_set_state_async(lj_system* s, const double* pos, const double* vel)
   return LJ_OK;
 }
 
-// Packs the requested arrays (one launch) and queues their copies to the
-// host behind the pending work; the caller synchronises.
-static lj_status enqueue_state_read(lj_system* s, double* pos, double* vel, double* force) {
+// Queues the read-back of the requested arrays behind the pending work, with
+// the status words and, with `scalars`, the per-box scalar block into h_sc:
+// one pack launch writes page-locked mapped destinations directly and the
+// status words and scalars into the handle's mapped mirrors; other
+// destinations get staged copies.  The caller finishes with finish_status.
+static lj_status enqueue_read(lj_system* s, double* pos, double* vel, double* force, bool scalars) {
   const size_t n3 = 3 * (size_t)s->ntotal;
   const double* src[3] = {s->x.p, s->v.p, s->f.p};
   double* dst[3] = {pos, vel, force};
@@ -1156,14 +1205,38 @@ static lj_status enqueue_state_read(lj_system* s, double* pos, double* vel, doub
   for (int k = 0; k < 3; ++k) {
     if (!dst[k]) continue;
     xa.src[na] = src[k];
-    xa.dst[na] = s->stage.p + na * n3;
-    host[na++] = dst[k];
+    double* d = static_cast<double*>(mapped_device_ptr(dst[k]));
+    if (d) {
+      xa.dst[na] = d;
+    } else {
+      xa.dst[na] = s->stage.p + na * n3;
+      host[na] = dst[k];
+    }
+    ++na;
   }
-  if (na == 0) return LJ_OK;
-  LJ_CUDA(s, launch_pack_multi(xa, na, s->ntotal, s->npad, s->stream));
-  s->launches += 1;
+  const bool mailbox = s->h_words.dev && (!scalars || s->h_sc.dev);
+  Mailbox mb{};
+  if (mailbox) {
+    mb.status = s->status.p;
+    mb.bad = s->upload_check_pending ? s->bad.p : nullptr;
+    mb.words_out = static_cast<int*>(s->h_words.dev);
+    if (scalars) {
+      mb.sc = reinterpret_cast<const int*>(s->sc.p);
+      mb.sc_out = static_cast<int*>(s->h_sc.dev);
+      mb.sc_nwords = (int)(sizeof(DevScalars) * s->nsys / sizeof(int));
+    }
+  }
+  LJ_CUDA(s, launch_pack_multi(xa, na, s->ntotal, s->npad, mailbox ? &mb : nullptr, s->stream));
+  if (na > 0 || mailbox) s->launches += 1;
   for (int k = 0; k < na; ++k)
-    LJ_CUDA(s, cudaMemcpyAsync(host[k], xa.dst[k], sizeof(double) * n3, cudaMemcpyDeviceToHost, s->stream));
+    if (host[k])
+      LJ_CUDA(s, cudaMemcpyAsync(host[k], xa.dst[k], sizeof(double) * n3, cudaMemcpyDeviceToHost, s->stream));
+  if (!mailbox) {
+    if (scalars)
+      LJ_CUDA(s, cudaMemcpyAsync(s->h_sc.p, s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost,
+                                 s->stream));
+    return enqueue_status_read(s);
+  }
   return LJ_OK;
 }
 
@@ -1174,9 +1247,8 @@ lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
   DeviceGuard device_guard(s->device);
   lj_status st = flush_observables(s);
   if (st) return st;
-  st = enqueue_state_read(s, pos, vel, force);
-  if (st) return st;
-  return sync_status(s);
+  if ((st = enqueue_read(s, pos, vel, force, false))) return st;
+  return finish_status(s);
 }
 
 // lj_get_state and lj_get_observables behind a single synchronisation.
@@ -1185,14 +1257,22 @@ lj_status lj_get_state_observables(lj_system* s, double* pos, double* vel, doubl
   DeviceGuard device_guard(s->device);
   lj_status st = flush_observables(s);
   if (st) return st;
-  st = enqueue_state_read(s, pos, vel, force);
-  if (st) return st;
-  if (out)
-    LJ_CUDA(s, cudaMemcpyAsync(s->h_sc.p, s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
-  st = sync_status(s);
-  if (st) return st;
+  if ((st = enqueue_read(s, pos, vel, force, out != nullptr))) return st;
+  if ((st = finish_status(s))) return st;
   if (out) fill_obs(s->h_sc.p[0], out);
   return LJ_OK;
+}
+
+// One host round trip of a caller that keeps the state on the host: queued
+// upload, steps, and the read-back with the observables, one synchronisation.
+lj_status lj_step_io(lj_system* s, const double* pos_in, const double* vel_in, double dt, int32_t nsteps,
+                     double* pos_out, double* vel_out, double* force_out, lj_observables* out) {
+  if (!s) return LJ_ERR_INVALID;
+  DeviceGuard device_guard(s->device);
+  lj_status st = lj_set_state_async(s, pos_in, vel_in);
+  if (st) return st;
+  if ((st = lj_step(s, dt, nsteps))) return st;
+  return lj_get_state_observables(s, pos_out, vel_out, force_out, out);
 }
 
 lj_status lj_get_pair_sums(lj_system* s, double* e, double* w) {

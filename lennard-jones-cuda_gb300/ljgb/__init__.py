@@ -78,6 +78,7 @@ def _declare(L):
         "lj_reinitialize": (C.c_int, [_P, C.POINTER(Config)]),
         "lj_set_state": (C.c_int, [_P, _P, _P]),
         "lj_set_state_async": (C.c_int, [_P, _P, _P]),
+        "lj_step_io": (C.c_int, [_P, _P, _P, C.c_double, C.c_int32, _P, _P, _P, C.POINTER(Observables)]),
         "lj_get_state": (C.c_int, [_P, _P, _P, _P]),
         "lj_get_pair_sums": (C.c_int, [_P, _P, _P]),
         "lj_compute_forces": (C.c_int, [_P]),
@@ -352,6 +353,18 @@ class System:
         (and alive) until the next synchronising call returns."""
         ptr = lambda a: a.ctypes.data if a is not None else None
         self._c(load().lj_set_state_async(self.h, ptr(pos), ptr(vel)))
+
+    def step_io(self, dt: float, nsteps: int = 1, pos_in=None, vel_in=None, pos_out=None, vel_out=None,
+                frc_out=None) -> dict:
+        """lj_step_io: queued upload of pos_in / vel_in, nsteps steps, the
+        state into the *_out buffers and the observables, one
+        synchronisation.  Inputs must stay alive and unchanged until it
+        returns (it returns after the synchronisation)."""
+        ptr = lambda a: a.ctypes.data if a is not None else None
+        o = Observables()
+        self._c(load().lj_step_io(self.h, ptr(pos_in), ptr(vel_in), float(dt), int(nsteps), ptr(pos_out),
+                                  ptr(vel_out), ptr(frc_out), C.byref(o)))
+        return o.as_dict()
 
     def pair_sums(self):
         e = np.zeros(self.ntotal)

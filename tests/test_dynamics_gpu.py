@@ -330,6 +330,48 @@ def test_set_state_async(ljgb_mod, boundary):
     b.close()
 
 
+@pytest.mark.parametrize("boundary", [0, 1])
+def test_step_io_matches_separate_calls(ljgb_mod, boundary):
+    """lj_step_io (queued upload, steps, read-back and observables, one
+    synchronisation) gives what lj_set_state + lj_step +
+    lj_get_state_observables give, bit for bit: with page-locked buffers (the
+    kernels read and write them directly) and with pageable ones (staged
+    copies).  A non-finite input is reported by the same call."""
+    n = 1100
+    kw = dict(n=n, density=0.75, temperature=1.2, canonical=1, boundary=boundary,
+              lattice=ljgb_mod.LATTICE_FCC, jitter=0.02, seed=9)
+    a, b, c = ljgb_mod.System(**kw), ljgb_mod.System(**kw), ljgb_mod.System(**kw)
+    pa, va = ljgb_mod.pinned((n, 3)), ljgb_mod.pinned((n, 3))
+    pc, vc = np.zeros((n, 3)), np.zeros((n, 3))
+    a.get_state_into(pa, va, None)
+    c.get_state_into(pc, vc, None)
+    pb, vb, _ = b.get_state()
+    for _ in range(5):
+        va *= 0.999
+        vb *= 0.999
+        vc *= 0.999
+        oa = a.step_io(0.005, 2, pa, va, pa, va)
+        oc = c.step_io(0.005, 2, pc, vc, pc, vc)
+        b.set_state(pb, vb)
+        b.integrate(0.005, 2)
+        ob = b.get_state_observables_into(pb, vb, None)
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+        assert np.array_equal(pc, pb) and np.array_equal(vc, vb)
+        assert oa["U"] == ob["U"] == oc["U"] and oa["step"] == ob["step"] == oc["step"]
+    fa = ljgb_mod.pinned((n, 3))
+    a.step_io(0.005, 1, None, None, None, None, fa)
+    b.integrate(0.005, 1)
+    _, _, fb = b.get_state()
+    assert np.array_equal(fa, fb)
+    va[3, 2] = np.inf
+    with pytest.raises(ljgb_mod.LJError, match="lj_set_state_async"):
+        a.step_io(0.005, 1, pa, va, pa, va)
+    a.integrate(0.005, 1)
+    assert np.isfinite(a.observables()["U"])
+    for s in (a, b, c):
+        s.close()
+
+
 def test_walls_frame_follows_set_state(ljgb_mod):
     """A walled box's fixed frame is rebuilt around positions set from the
     host, even far outside the walls; the wall turns the particle back."""
