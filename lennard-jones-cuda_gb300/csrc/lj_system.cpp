@@ -1934,14 +1934,26 @@ lj_status lj_autotune(lj_system* s) {
       prev_G = s->sched.G;
       if ((st = restore())) return give_up(st);
       if ((st = enqueue_compute_forces(s))) return give_up(st);
-      if ((st = lj_step(s, dt, 2))) return give_up(st);
+      // two warm-up steps (timed, to size the rounds), then the fastest of
+      // three rounds of about 1 ms each (2..10 steps): neighbouring shapes
+      // differ by ~1%, about the spread of a single short round
       LJ_CUDA(s, cudaEventRecord(e0, s->stream));
-      const int reps = 6;
-      if ((st = lj_step(s, dt, reps))) return give_up(st);
+      if ((st = lj_step(s, dt, 2))) return give_up(st);
       LJ_CUDA(s, cudaEventRecord(e1, s->stream));
       LJ_CUDA(s, cudaEventSynchronize(e1));
-      float ms = 0;
-      LJ_CUDA(s, cudaEventElapsedTime(&ms, e0, e1));
+      float warm_ms = 0;
+      LJ_CUDA(s, cudaEventElapsedTime(&warm_ms, e0, e1));
+      const int reps = std::max(2, std::min(10, (int)(1.0f / std::max(warm_ms * 0.5f, 1e-3f))));
+      float ms = 1e30f;
+      for (int round = 0; round < 3; ++round) {
+        LJ_CUDA(s, cudaEventRecord(e0, s->stream));
+        if ((st = lj_step(s, dt, reps))) return give_up(st);
+        LJ_CUDA(s, cudaEventRecord(e1, s->stream));
+        LJ_CUDA(s, cudaEventSynchronize(e1));
+        float r_ms = 0;
+        LJ_CUDA(s, cudaEventElapsedTime(&r_ms, e0, e1));
+        ms = std::min(ms, r_ms / reps);
+      }
       if ((st = check_status(s))) return give_up(st);
       if (ms < best_ms) {
         best_ms = ms;
