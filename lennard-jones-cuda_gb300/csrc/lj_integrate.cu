@@ -537,11 +537,14 @@ __global__ void k_unpack(const double* __restrict__ in, double* __restrict__ out
   for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
 }
 
-// Up to three (N,3) <-> component-major transposes in one launch; blockIdx.y
-// selects the array.  With a mailbox, the row after the arrays copies the
-// status words and the scalar block into the handle's page-locked mirrors
-// (destinations may be mapped host memory: the host reads them after one
-// synchronisation, with no copy operation queued).
+// Up to three component-major [3][npad] -> (N,3) transposes in one launch;
+// blockIdx.y selects the array.  Thread k writes element k of the (N,3)
+// output (consecutive threads, consecutive doubles: whole-line stores, which
+// matters when the destination is host memory written over the chip-to-chip
+// link) and gathers it from the device array.  With a mailbox, the row after
+// the arrays copies the status words and the scalar block into the handle's
+// page-locked mirrors (destinations may be mapped host memory: the host reads
+// them after one synchronisation, with no copy operation queued).
 __global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb) {
   if ((int)blockIdx.y == count) {
     if (blockIdx.x != 0) return;
@@ -552,37 +555,39 @@ __global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb
     for (int k = threadIdx.x; k < mb.sc_nwords; k += blockDim.x) mb.sc_out[k] = mb.sc[k];
     return;
   }
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double* __restrict__ in = a.src[blockIdx.y];
-  double* __restrict__ out = a.dst[blockIdx.y];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) out[3 * (size_t)i + c] = in[(size_t)c * npad + i];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 3 * n) return;
+  const int i = k / 3, c = k - 3 * i;
+  a.dst[blockIdx.y][k] = a.src[blockIdx.y][(size_t)c * npad + i];
 }
 
-// k_unpack for up to three arrays, skipped when k_check_finite found a
-// non-finite value.
-__global__ void k_unpack_multi_checked(XyzArrays a, int n, int npad, const int* bad) {
+// First half of an upload: (N,3) positions (blockIdx.y = 0) and velocities
+// (1), either possibly host memory mapped into the device's address space,
+// read once with whole-line loads; each value is checked (lowest index of a
+// non-finite value into *bad, velocities after the na position values) and
+// written component-major into the staging buffer.
+__global__ void k_upload_stage(const double* __restrict__ pos, const double* __restrict__ vel, int n, int npad,
+                               double* __restrict__ spos, double* __restrict__ svel, int na, int* bad) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const double* src = blockIdx.y == 0 ? pos : vel;
+  if (!src || k >= 3 * n) return;
+  const double x = src[k];
+  if (!isfinite(x)) atomicMin(bad, blockIdx.y == 0 ? k : na + k);
+  const int i = k / 3, c = k - 3 * i;
+  (blockIdx.y == 0 ? spos : svel)[(size_t)c * npad + i] = x;
+}
+
+// Second half: the staged arrays become the state, unless a value was not
+// finite (all or nothing).  Component-major on both sides: plain copies.
+__global__ void k_upload_commit(const double* __restrict__ spos, const double* __restrict__ svel, double* x,
+                                double* v, int n, int npad, const int* bad) {
   if (*bad != 0x7f7f7f7f) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double* __restrict__ in = a.src[blockIdx.y];
-  double* __restrict__ out = a.dst[blockIdx.y];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) out[(size_t)c * npad + i] = in[3 * (size_t)i + c];
-}
-
-// Lowest index of a non-finite value among the na values of a followed by
-// the nb values of b (bad starts at 0x7f7f7f7f); blockIdx.y selects the
-// array.  Either may be host memory mapped into the device's address space.
-__global__ void k_check_finite2(const double* __restrict__ a, long long na, const double* __restrict__ b,
-                                long long nb, int* bad) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (blockIdx.y == 0) {
-    if (i < na && !isfinite(a[i])) atomicMin(bad, (int)i);
-  } else if (i < nb && !isfinite(b[i])) {
-    atomicMin(bad, (int)(na + i));
-  }
+  const double* src = blockIdx.y == 0 ? spos : svel;
+  if (!src) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= 3 * npad) return;
+  const int c = j / npad, i = j - c * npad;
+  if (i < n) (blockIdx.y == 0 ? x : v)[j] = src[j];
 }
 
 // A wait that nothing completes: the pair kernels' bounded mbarrier wait must
@@ -608,13 +613,6 @@ cudaError_t launch_selftest_wait(int* status, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_check_finite2(const double* a, size_t na, const double* b, size_t nb, int* bad, cudaStream_t st) {
-  const size_t m = na > nb ? na : nb;
-  if (m == 0) return cudaSuccess;
-  k_check_finite2<<<dim3((unsigned)((m + 255) / 256), 2), 256, 0, st>>>(a, (long long)na, b, (long long)nb, bad);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st) {
   k_unpack<<<(n + 255) / 256, 256, 0, st>>>(in, out, n, npad);
   return cudaGetLastError();
@@ -623,14 +621,20 @@ cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaSt
 cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, cudaStream_t st) {
   const int rows = count + (mb ? 1 : 0);
   if (rows <= 0) return cudaSuccess;
-  k_pack_multi<<<dim3((n + 255) / 256, rows), 256, 0, st>>>(a, count, n, npad, mb ? *mb : Mailbox{});
+  k_pack_multi<<<dim3((3 * n + 255) / 256, rows), 256, 0, st>>>(a, count, n, npad, mb ? *mb : Mailbox{});
   return cudaGetLastError();
 }
 
-cudaError_t launch_unpack_multi_checked(const XyzArrays& a, int count, int n, int npad, const int* bad,
-                                        cudaStream_t st) {
-  if (count <= 0) return cudaSuccess;
-  k_unpack_multi_checked<<<dim3((n + 255) / 256, count), 256, 0, st>>>(a, n, npad, bad);
+cudaError_t launch_upload(const double* pos, const double* vel, int n, int npad, double* stage_cm, double* x,
+                          double* v, int* bad, cudaStream_t st) {
+  if (!pos && !vel) return cudaSuccess;
+  double* spos = pos ? stage_cm : nullptr;
+  double* svel = vel ? stage_cm + 3 * (size_t)npad : nullptr;
+  const int na = pos ? 3 * n : 0;
+  k_upload_stage<<<dim3((3 * n + 255) / 256, 2), 256, 0, st>>>(pos, vel, n, npad, spos, svel, na, bad);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_upload_commit<<<dim3((3 * npad + 255) / 256, 2), 256, 0, st>>>(spos, svel, x, v, n, npad, bad);
   return cudaGetLastError();
 }
 

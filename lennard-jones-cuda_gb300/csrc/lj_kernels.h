@@ -149,9 +149,6 @@ cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, in
                             cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_selftest_wait(int* status, cudaStream_t st);
-// Lowest index of a non-finite value in a[0..na) then b[0..nb) (index na + k
-// for b[k]); either array may be mapped host memory.
-cudaError_t launch_check_finite2(const double* a, size_t na, const double* b, size_t nb, int* bad, cudaStream_t st);
 // Up to three (N,3) interleaved <-> component-major [3][npad] transposes in one launch.
 struct XyzArrays {
   const double* src[3];
@@ -169,8 +166,13 @@ struct Mailbox {
   int sc_nwords;
 };
 cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, cudaStream_t st);
-cudaError_t launch_unpack_multi_checked(const XyzArrays& a, int count, int n, int npad, const int* bad,
-                                        cudaStream_t st);
+// Upload of (N,3) positions / velocities (either may be NULL; either may be
+// mapped host memory): checked and staged component-major in stage_cm (6 npad
+// doubles), then committed into x / v only if every value was finite; *bad
+// receives the lowest index of a non-finite value (velocities after the 3n
+// position values) and must hold 0x7f7f7f7f before.
+cudaError_t launch_upload(const double* pos, const double* vel, int n, int npad, double* stage_cm, double* x,
+                          double* v, int* bad, cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,
                                     cudaStream_t st);
 

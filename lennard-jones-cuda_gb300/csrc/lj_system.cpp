@@ -832,7 +832,7 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, s->v.alloc(n3));
   LJ_CUDA(s, s->f.alloc(n3));
   LJ_CUDA(s, s->tf.alloc(n3));
-  LJ_CUDA(s, s->stage.alloc(3 * n3));
+  LJ_CUDA(s, s->stage.alloc(4 * n3));  // uploads: 2 (N,3) + 2 component-major arrays; reads: 3 (N,3)
   LJ_CUDA(s, s->bad.alloc(1));
   LJ_CUDA(s, s->h_words.alloc(2));
   LJ_CUDA(s, s->h_sc.alloc(s->nsys));
@@ -1116,15 +1116,18 @@ lj_status lj_reinitialize(lj_system* s, const lj_config* cfg) {
 // the device; the state is written only if every value is finite, so a
 // rejected call leaves it unchanged.  One synchronisation (the caller's
 // buffers are free on return).
-// Queues the upload of pos / vel through the staging buffer: copies, the
-// finiteness check (lowest bad index into s->bad) and the checked unpack.
+// Queues the upload of pos / vel: the finiteness check (lowest bad index into
+// s->bad) with the transpose into the staging buffer, then the commit.
 // A check still pending from an earlier queued upload keeps its index, so a
 // rejection is never lost (later uploads are then dropped too).
 // Page-locked mapped caller buffers are read by the kernels directly; others
-// are copied to the staging buffer first.
+// are copied to the staging buffer first.  Staging buffer: [0, 6 npad) the
+// copied (N,3) host arrays, [6 npad, 12 npad) the component-major arrays
+// checked before they are committed.
 static lj_status enqueue_upload(lj_system* s, const double* pos, const double* vel) {
   s->pred_ready = false;
   const size_t n3 = 3 * (size_t)s->ntotal;
+  const size_t pad3 = 3 * (size_t)s->npad;
   const double* src_pos = static_cast<const double*>(mapped_device_ptr(pos));
   const double* src_vel = static_cast<const double*>(mapped_device_ptr(vel));
   if (!s->upload_check_pending) LJ_CUDA(s, cudaMemsetAsync(s->bad.p, 0x7f, sizeof(int), s->stream));
@@ -1133,21 +1136,11 @@ static lj_status enqueue_upload(lj_system* s, const double* pos, const double* v
     src_pos = s->stage.p;
   }
   if (vel && !src_vel) {
-    LJ_CUDA(s, cudaMemcpyAsync(s->stage.p + n3, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
-    src_vel = s->stage.p + n3;
+    LJ_CUDA(s, cudaMemcpyAsync(s->stage.p + pad3, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
+    src_vel = s->stage.p + pad3;
   }
-  LJ_CUDA(s, launch_check_finite2(src_pos, pos ? n3 : 0, src_vel, vel ? n3 : 0, s->bad.p, s->stream));
-  XyzArrays xa{};
-  int na = 0;
-  if (pos) {
-    xa.src[na] = src_pos;
-    xa.dst[na++] = s->x.p;
-  }
-  if (vel) {
-    xa.src[na] = src_vel;
-    xa.dst[na++] = s->v.p;
-  }
-  LJ_CUDA(s, launch_unpack_multi_checked(xa, na, s->ntotal, s->npad, s->bad.p, s->stream));
+  LJ_CUDA(s, launch_upload(pos ? src_pos : nullptr, vel ? src_vel : nullptr, s->ntotal, s->npad,
+                           s->stage.p + 2 * pad3, s->x.p, s->v.p, s->bad.p, s->stream));
   s->launches += 2;
   return LJ_OK;
 }
