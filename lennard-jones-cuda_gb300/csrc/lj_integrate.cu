@@ -550,7 +550,10 @@ __global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb
     if (blockIdx.x != 0) return;
     if (threadIdx.x == 0) {
       mb.words_out[0] = *mb.status;
-      if (mb.bad) mb.words_out[1] = *mb.bad;
+      if (mb.bad) {
+        mb.words_out[1] = *mb.bad;
+        *mb.bad = 0x7f7f7f7f;  // read: ready for the next upload's check
+      }
     }
     for (int k = threadIdx.x; k < mb.sc_nwords; k += blockDim.x) mb.sc_out[k] = mb.sc[k];
     return;
@@ -577,17 +580,32 @@ __global__ void k_upload_stage(const double* __restrict__ pos, const double* __r
   (blockIdx.y == 0 ? spos : svel)[(size_t)c * npad + i] = x;
 }
 
-// Second half: the staged arrays become the state, unless a value was not
-// finite (all or nothing).  Component-major on both sides: plain copies.
-__global__ void k_upload_commit(const double* __restrict__ spos, const double* __restrict__ svel, double* x,
-                                double* v, int n, int npad, const int* bad) {
-  if (*bad != 0x7f7f7f7f) return;
-  const double* src = blockIdx.y == 0 ? spos : svel;
-  if (!src) return;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= 3 * npad) return;
-  const int c = j / npad, i = j - c * npad;
-  if (i < n) (blockIdx.y == 0 ? x : v)[j] = src[j];
+// Second half, one thread per particle on the i-block decomposition: the
+// staged arrays become the state unless a value was not finite (all or
+// nothing).  With `predict` (periodic boxes on the fused step) the same thread
+// then writes the next pair kernel's shadow x + dt v + dt^2 F / 2, as
+// k_predict does, so the first step after an upload needs no predictor launch.
+__global__ void k_upload_commit(StateArgs s, const double* __restrict__ spos, const double* __restrict__ svel,
+                                const int* bad, int predict) {
+  const BlockInfo bi = s.blocks[blockIdx.x];
+  if ((int)threadIdx.x >= bi.n_i) return;
+  const int p = bi.p0 + bi.i0 + threadIdx.x;
+  const bool ok = *bad == 0x7f7f7f7f;
+  double x[3], v[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = (size_t)c * s.npad + p;
+    x[c] = (ok && spos) ? spos[k] : s.x[k];
+    v[c] = (ok && svel) ? svel[k] : s.v[k];
+    if (ok && spos) s.x[k] = x[c];
+    if (ok && svel) s.v[k] = v[c];
+  }
+  if (!predict) return;
+  const BoxArgs box = s.boxes[bi.sys];
+  double xp[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) xp[c] = drift_pos(box, x[c], v[c], s.f[(size_t)c * s.npad + p]);
+  s.q[p] = shadow_of(s.sc[bi.sys], xp[0], xp[1], xp[2]);
 }
 
 // A wait that nothing completes: the pair kernels' bounded mbarrier wait must
@@ -625,16 +643,17 @@ cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, co
   return cudaGetLastError();
 }
 
-cudaError_t launch_upload(const double* pos, const double* vel, int n, int npad, double* stage_cm, double* x,
-                          double* v, int* bad, cudaStream_t st) {
+cudaError_t launch_upload_stage(const double* pos, const double* vel, int n, int npad, double* spos, double* svel,
+                                int* bad, cudaStream_t st) {
   if (!pos && !vel) return cudaSuccess;
-  double* spos = pos ? stage_cm : nullptr;
-  double* svel = vel ? stage_cm + 3 * (size_t)npad : nullptr;
   const int na = pos ? 3 * n : 0;
   k_upload_stage<<<dim3((3 * n + 255) / 256, 2), 256, 0, st>>>(pos, vel, n, npad, spos, svel, na, bad);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_upload_commit<<<dim3((3 * npad + 255) / 256, 2), 256, 0, st>>>(spos, svel, x, v, n, npad, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_upload_commit(const StateArgs& s, int nblocks, int bi, const double* spos, const double* svel,
+                                 const int* bad, bool predict, cudaStream_t st) {
+  k_upload_commit<<<nblocks, bi, 0, st>>>(s, spos, svel, bad, predict ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -155,11 +155,11 @@ struct XyzArrays {
   double* dst[3];
 };
 // Small device words copied by the pack launch: the status word (and the
-// upload check's bad index, if bad is set) to words_out[0..1], and
-// sc_nwords 32-bit words of the scalar block to sc_out.
+// upload check's bad index, if bad is set, which is then reset to 0x7f7f7f7f)
+// to words_out[0..1], and sc_nwords 32-bit words of the scalar block to sc_out.
 struct Mailbox {
   const int* status;
-  const int* bad;
+  int* bad;
   int* words_out;
   const int* sc;
   int* sc_out;
@@ -167,12 +167,16 @@ struct Mailbox {
 };
 cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, cudaStream_t st);
 // Upload of (N,3) positions / velocities (either may be NULL; either may be
-// mapped host memory): checked and staged component-major in stage_cm (6 npad
-// doubles), then committed into x / v only if every value was finite; *bad
-// receives the lowest index of a non-finite value (velocities after the 3n
-// position values) and must hold 0x7f7f7f7f before.
-cudaError_t launch_upload(const double* pos, const double* vel, int n, int npad, double* stage_cm, double* x,
-                          double* v, int* bad, cudaStream_t st);
+// mapped host memory), in two launches.  Stage: every value checked (*bad
+// receives the lowest index of a non-finite value, velocities after the 3n
+// position values; it must hold 0x7f7f7f7f before) and written component-major
+// to spos / svel ([3][npad] each).  Commit (grid = i-blocks): the staged
+// arrays become x / v only if every value was finite; with `predict`, also
+// the fused step's shadow of x + dt v + dt^2 F / 2 into s.q (periodic boxes).
+cudaError_t launch_upload_stage(const double* pos, const double* vel, int n, int npad, double* spos, double* svel,
+                                int* bad, cudaStream_t st);
+cudaError_t launch_upload_commit(const StateArgs& s, int nblocks, int bi, const double* spos, const double* svel,
+                                 const int* bad, bool predict, cudaStream_t st);
 cudaError_t launch_scale_velocities(const StateArgs& s, int nblocks, int bi, int sysmode, double target,
                                     cudaStream_t st);
 

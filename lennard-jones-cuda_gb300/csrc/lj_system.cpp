@@ -223,6 +223,7 @@ struct lj_system {
   DevBuf<int> bad;               // lowest index of a non-finite uploaded value (INT_MAX: none)
   PinnedBuf<int> h_words;        // [0] status, [1] bad index: read back after one synchronisation
   bool upload_check_pending = false;  // lj_set_state_async queued a finiteness check not yet read back
+  bool bad_clean = false;             // s->bad holds 0x7f7f7f7f (reset by the read-back of a check)
   PinnedBuf<DevScalars> h_sc;    // per-box scalars read back
   DevBuf<int4> q, q2;  // fixed-point shadow, double-buffered for the fused step
   DevBuf<double4_32a> xd;
@@ -1130,7 +1131,9 @@ static lj_status enqueue_upload(lj_system* s, const double* pos, const double* v
   const size_t pad3 = 3 * (size_t)s->npad;
   const double* src_pos = static_cast<const double*>(mapped_device_ptr(pos));
   const double* src_vel = static_cast<const double*>(mapped_device_ptr(vel));
-  if (!s->upload_check_pending) LJ_CUDA(s, cudaMemsetAsync(s->bad.p, 0x7f, sizeof(int), s->stream));
+  if (!s->upload_check_pending && !s->bad_clean)
+    LJ_CUDA(s, cudaMemsetAsync(s->bad.p, 0x7f, sizeof(int), s->stream));
+  s->bad_clean = false;
   if (pos && !src_pos) {
     LJ_CUDA(s, cudaMemcpyAsync(s->stage.p, pos, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
     src_pos = s->stage.p;
@@ -1139,9 +1142,21 @@ static lj_status enqueue_upload(lj_system* s, const double* pos, const double* v
     LJ_CUDA(s, cudaMemcpyAsync(s->stage.p + pad3, vel, sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream));
     src_vel = s->stage.p + pad3;
   }
-  LJ_CUDA(s, launch_upload(pos ? src_pos : nullptr, vel ? src_vel : nullptr, s->ntotal, s->npad,
-                           s->stage.p + 2 * pad3, s->x.p, s->v.p, s->bad.p, s->stream));
+  double* spos = pos ? s->stage.p + 2 * pad3 : nullptr;
+  double* svel = vel ? s->stage.p + 3 * pad3 : nullptr;
+  LJ_CUDA(s, launch_upload_stage(pos ? src_pos : nullptr, vel ? src_vel : nullptr, s->ntotal, s->npad, spos, svel,
+                                 s->bad.p, s->stream));
+  // Periodic boxes on the fused step keep a fixed frame: the commit also
+  // writes the predictor for the last step size used, so the next step needs
+  // no predictor launch (a walled box's frame is rebuilt around the new
+  // positions first, and its predictor follows at the step).
+  const bool predict = use_fused(s) && !s->any_nonperiodic && s->boxes[0].dt > 0;
+  LJ_CUDA(s, launch_upload_commit(state_args(s), nblocks(s), s->BI, spos, svel, s->bad.p, predict, s->stream));
   s->launches += 2;
+  if (predict) {
+    s->pred_ready = true;
+    s->pred_dt = s->boxes[0].dt;
+  }
   return LJ_OK;
 }
 
@@ -1212,6 +1227,7 @@ static lj_status enqueue_read(lj_system* s, double* pos, double* vel, double* fo
   if (mailbox) {
     mb.status = s->status.p;
     mb.bad = s->upload_check_pending ? s->bad.p : nullptr;
+    if (mb.bad) s->bad_clean = true;  // the pack launch resets it after reading
     mb.words_out = static_cast<int*>(s->h_words.dev);
     if (scalars) {
       mb.sc = reinterpret_cast<const int*>(s->sc.p);

@@ -372,6 +372,32 @@ def test_step_io_matches_separate_calls(ljgb_mod, boundary):
         s.close()
 
 
+def test_upload_writes_the_predictor(ljgb_mod):
+    """On periodic boxes the upload's commit also writes the fused step's
+    predictor, so the step after an upload launches no predictor kernel; a
+    round trip of the state through host memory then leaves the trajectory
+    bit-identical to a twin that never left the GPU."""
+    kw = dict(n=1500, density=0.8, temperature=1.0, canonical=1, lattice=ljgb_mod.LATTICE_FCC, jitter=0.02, seed=3)
+    a, b = ljgb_mod.System(**kw), ljgb_mod.System(**kw)
+    a.integrate(0.005, 3)
+    b.integrate(0.005, 3)
+    for _ in range(4):
+        p, v, _ = a.get_state()
+        c0 = a.launch_count()
+        a.set_state_async_from(p, v)
+        a.integrate(0.005)
+        b.integrate(0.005)
+        a.sync()
+        b.sync()
+        assert a.launch_count() - c0 == 2 + 2          # stage + commit, pairs + TVN close
+    pa, va, fa = a.get_state()
+    pb, vb, fb = b.get_state()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+    assert a.observables()["U"] == b.observables()["U"]
+    a.close()
+    b.close()
+
+
 def test_walls_frame_follows_set_state(ljgb_mod):
     """A walled box's fixed frame is rebuilt around positions set from the
     host, even far outside the walls; the wall turns the particle back."""
