@@ -389,7 +389,8 @@ def test_upload_writes_the_predictor(ljgb_mod):
         b.integrate(0.005)
         a.sync()
         b.sync()
-        assert a.launch_count() - c0 == 2 + 2          # stage + commit, pairs + TVN close
+        # stage + commit, pairs + TVN close, the step's observables at the sync
+        assert a.launch_count() - c0 == 2 + 2 + 1
     pa, va, fa = a.get_state()
     pb, vb, fb = b.get_state()
     assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
