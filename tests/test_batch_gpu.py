@@ -2,7 +2,7 @@
 T* and boundaries advanced together -- one persistent pair launch per step
 covers every box.  Each box must evolve exactly as it would alone (same
 initial state from the same config, same equations), up to the summation
-order of the FP32 pair sums."""
+order of the FP32 pair sums, and as the FP64 oracle steps it."""
 import numpy as np
 import pytest
 
@@ -39,6 +39,37 @@ def test_batch_matches_individual_boxes(ljgb_mod, canonical):
         for key in ("K", "V", "T", "P", "U", "t"):
             assert ob[k][key] == pytest.approx(o[key], rel=1e-6, abs=1e-6), (k, key)
         assert ob[k]["step"] == 20
+
+
+@pytest.mark.parametrize("canonical", [1, 0], ids=["tvn", "evn"])
+def test_batch_boxes_match_fp64_oracle(ljgb_mod, oracle_mod, canonical):
+    """Each box of a batch (uneven N, rho*, T*, periodic and hard-wall boxes)
+    against the FP64 oracle restatement of the reference's step, directly:
+    20 steps of dt 0.004 from the batch's own initial state."""
+    cfgs = make_cfgs(ljgb_mod, 6, seed=17, canonical=canonical, n_range=(200, 900))
+    b = ljgb_mod.System(batch=cfgs)
+    p0, v0, _ = b.get_state()
+    oracles = []
+    for k, c in enumerate(cfgs):
+        sl = slice(b.offsets[k], b.offsets[k + 1])
+        L = (c.n / c.density) ** (1 / 3)
+        oracles.append(oracle_mod.F64System(p0[sl], v0[sl], L, c.density, c.temperature, bool(canonical),
+                                            c.boundary, nthreads=4))
+    steps = 20
+    b.integrate(0.004, steps)
+    for o in oracles:
+        for _ in range(steps):
+            o.step(0.004)
+    p, v, _ = b.get_state()
+    obs = b.batch_observables()
+    for k, (c, o) in enumerate(zip(cfgs, oracles)):
+        sl = slice(b.offsets[k], b.offsets[k + 1])
+        L = (c.n / c.density) ** (1 / 3)
+        assert np.abs(p[sl] - o.pos).max() < 1e-6 * max(1.0, L), k
+        assert np.abs(v[sl] - o.vel).max() < 1e-5, k
+        for key in ("K", "V", "T", "P", "U"):
+            assert obs[k][key] == pytest.approx(getattr(o, key), rel=1e-5, abs=1e-5 * c.n), (k, key)
+        assert obs[k]["step"] == steps
 
 
 def test_batch_periodic_only_uses_fused_step(ljgb_mod):
