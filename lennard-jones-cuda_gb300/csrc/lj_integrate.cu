@@ -442,7 +442,30 @@ __global__ void k_obs_finalize(StateArgs s) {
 //   slab (type t < 3):  k = (int)((x_t / L) / alpha_step)
 //   cube (type 3):      k = max over axes of #{tl_j <= |x_c - L/2| / 0.5}
 //   velocity (4 .. 6):  k = (int)((|v_c| / vmax) / alpha_step)
-__global__ void k_counters(StateArgs s, const CounterDev* cs, int nc, int nbins, int* row, int n) {
+// Per-step bookkeeping of the counters, before k_counters (one CTA): whether
+// this step is counted (every `every`-th step) and into which ring row; that
+// row is cleared here.  st: CounterState words.  On the device, so the
+// counters run inside the captured step graph.
+__global__ void k_counter_prep(int* st, int* ring, int nbins) {
+  __shared__ int row;
+  if (threadIdx.x == 0) {
+    row = -1;
+    if (++st[kCtrPhase] >= st[kCtrEvery]) {
+      st[kCtrPhase] = 0;
+      row = st[kCtrNext];
+      st[kCtrNext] = row + 1 == st[kCtrCap] ? 0 : row + 1;
+    }
+    st[kCtrRow] = row;
+  }
+  __syncthreads();
+  if (row >= 0)
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) ring[(size_t)row * nbins + b] = 0;
+}
+
+__global__ void k_counters(StateArgs s, const CounterDev* cs, int nc, int nbins, const int* st, int* ring, int n) {
+  const int r = st[kCtrRow];
+  if (r < 0) return;  // not a counted step
+  int* row = ring + (size_t)r * nbins;
   extern __shared__ int shc[];
   for (int b = threadIdx.x; b < nbins; b += blockDim.x) shc[b] = 0;
   __syncthreads();
@@ -708,10 +731,13 @@ cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* row, int n,
+cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* state, int* ring, int n,
                             cudaStream_t st) {
+  k_counter_prep<<<1, 256, 0, st>>>(state, ring, nbins);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
   const int threads = 256;
-  k_counters<<<(n + threads - 1) / threads, threads, sizeof(int) * nbins, st>>>(s, cs, nc, nbins, row, n);
+  k_counters<<<(n + threads - 1) / threads, threads, sizeof(int) * nbins, st>>>(s, cs, nc, nbins, state, ring, n);
   return cudaGetLastError();
 }
 

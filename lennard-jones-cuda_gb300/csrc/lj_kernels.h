@@ -143,9 +143,15 @@ struct CounterDev {
   double vmax;
   double tl[kMaxCounterAlphas];  // type 3: cube sides L alpha_k^(1/3)
 };
-// Histogram of the counters' bin indices over the particles of box 0, added
-// into row[0 .. nbins) (zeroed by the caller).
-cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* row, int n,
+// Device words of the counters (DevBuf<int> of kCtrWords): next ring row,
+// steps since the last counted one, the interval, the ring's rows, and the
+// row of the current step (-1: not counted).
+enum : int { kCtrNext = 0, kCtrPhase = 1, kCtrEvery = 2, kCtrCap = 3, kCtrRow = 4, kCtrWords = 8 };
+// One step of the counters, two launches (graph-capturable: everything that
+// changes per step lives in `state`): the bookkeeping, which clears the
+// step's ring row when the step is counted, then the histogram of the
+// counters' bin indices over the particles of box 0 added into that row.
+cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* state, int* ring, int n,
                             cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_selftest_wait(int* status, cudaStream_t st);

@@ -248,6 +248,7 @@ struct lj_system {
   std::vector<CounterDev> counters;
   DevBuf<CounterDev> dcounters;
   DevBuf<int> counter_ring;
+  DevBuf<int> counter_state;     // kCtr* words: the device's copy of the bookkeeping below
   int counter_bins = 0, counter_cap = 0;
   int counter_every = 1;         // count after every counter_every-th step
   long long counter_phase = 0;   // steps since the last counted one
@@ -562,6 +563,8 @@ lj_status hist_pass_args(lj_system* s, int shape, const int4* q, const HistArgs&
     s->h_cta_block.swap(cb);
     s->h_cta_jt.swap(cj);
     s->hsched = std::move(sch);
+    // step graphs that accumulate the RDF name the old tables (freed on return)
+    if (s->rdf_acc) clear_graphs(s);
     s->hist_shape = shape;
     s->hist_nb = h.nb;
   }
@@ -677,14 +680,26 @@ int step_mode(const lj_system* s) {
   return MODE_EVN;
 }
 
+lj_status enqueue_after_step(lj_system* s, const PairArgs* hist, int hist_grid, int* kernels);
+
 lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
   const bool fused = use_fused(s);
-  const int key = mode * 16 + (fused ? 8 : 0) + (fused && s->qpar ? 4 : 0) + (s->any_nonperiodic ? 2 : 0) +
-                  (s->profiling ? 1 : 0);
+  const bool counters = s->counter_cap > 0, rdf = s->rdf_acc;
+  const int key = mode * 128 + (rdf ? 64 : 0) + (counters ? 32 : 0) + (fused ? 8 : 0) + (fused && s->qpar ? 4 : 0) +
+                  (s->any_nonperiodic ? 2 : 0) + (s->profiling ? 1 : 0);
   auto it = s->graphs.find(key);
   if (it != s->graphs.end()) {
     *out = &it->second;
     return LJ_OK;
+  }
+  // The RDF pass's range tables are built before the capture (building them
+  // may allocate and synchronise).
+  PairArgs hist{};
+  int hist_grid = 0;
+  if (rdf) {
+    const int shape = (s->prec == LJ_PREC_MIXED) ? s->shape : 0;
+    lj_status hst = hist_pass_args(s, shape, s->qhist.p, s->rdf_args, &hist, &hist_grid);
+    if (hst) return hst;
   }
   GraphEntry ge;
   ge.profiled = s->profiling;
@@ -697,6 +712,7 @@ lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
   LJ_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   lj_status st = fused ? enqueue_step_fused(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels)
                        : enqueue_step(s, mode, ge.profiled ? ev : nullptr, true, &ge.kernels);
+  if (!st && (counters || rdf)) st = enqueue_after_step(s, &hist, hist_grid, &ge.kernels);
   cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
   if (st || ce != cudaSuccess) {  // nothing of a failed capture is kept
     if (g) cudaGraphDestroy(g);
@@ -745,32 +761,38 @@ lj_status flush_observables(lj_system* s) {
 
 // Work after every step: the subsystem counters and the summed RDF, when
 // enabled (plain launches after the step's graph).
-lj_status after_step(lj_system* s) {
-  if (s->counter_cap > 0 && ++s->counter_phase >= s->counter_every) {
-    s->counter_phase = 0;
-    int* row = s->counter_ring.p + (size_t)(s->counter_head % s->counter_cap) * s->counter_bins;
-    LJ_CUDA(s, cudaMemsetAsync(row, 0, sizeof(int) * s->counter_bins, s->stream));
-    LJ_CUDA(s, launch_counters(state_args(s), s->dcounters.p, (int)s->counters.size(), s->counter_bins, row,
-                               s->ntotal, s->stream));
-    s->counter_head += 1;
-    s->launches += 1;
+// The per-step work that follows a step when counters or RDF accumulation are
+// on, enqueued inside the step graph's capture (its per-step state -- ring
+// row, counting phase -- lives on the device): the counters' bookkeeping and
+// histogram, and the RDF of the step's positions (quantized into a shadow of
+// their own: the step's shadow buffer holds the next step's prediction) added
+// into the running sum.  `hist` are the histogram pass's arguments, prepared
+// before the capture.
+lj_status enqueue_after_step(lj_system* s, const PairArgs* hist, int hist_grid, int* kernels) {
+  if (s->counter_cap > 0) {
+    LJ_CUDA(s, launch_counters(state_args(s), s->dcounters.p, (int)s->counters.size(), s->counter_bins,
+                               s->counter_state.p, s->counter_ring.p, s->ntotal, s->stream));
+    *kernels += 2;
   }
   if (s->rdf_acc) {
-    // The step's shadow buffer holds the next step's prediction: quantize the
-    // current positions into a buffer of their own.
     StateArgs a = state_args(s);
     a.q = s->qhist.p;
     LJ_CUDA(s, launch_quantize(a, nblocks(s), s->BI, false, s->stream));
     const int shape = (s->prec == LJ_PREC_MIXED) ? s->shape : 0;
-    PairArgs p;
-    int grid = 0;
-    lj_status hst = hist_pass_args(s, shape, s->qhist.p, s->rdf_args, &p, &grid);
-    if (hst) return hst;
-    LJ_CUDA(s, launch_pairs(LJ_PREC_MIXED, shape, false, true, p, grid, s->stream));
-    s->rdf_samples += 1;
-    s->launches += 2;
+    LJ_CUDA(s, launch_pairs(LJ_PREC_MIXED, shape, false, true, *hist, hist_grid, s->stream));
+    *kernels += 2;
   }
   return LJ_OK;
+}
+
+// The host's mirror of that bookkeeping, after every launched step: the same
+// counting decision as k_counter_prep, and one more RDF sample.
+void after_step_host(lj_system* s) {
+  if (s->counter_cap > 0 && ++s->counter_phase >= s->counter_every) {
+    s->counter_phase = 0;
+    s->counter_head += 1;
+  }
+  if (s->rdf_acc) s->rdf_samples += 1;
 }
 
 // Waits for the handle's stream and reports the device status word, read
@@ -1066,6 +1088,7 @@ lj_status lj_destroy(lj_system* s) {
   s->cta_tile_begin.free();
   s->dcounters.free();
   s->counter_ring.free();
+  s->counter_state.free();
   s->rdf_sum.free();
   s->qhist.free();
   s->h_cta_tile_begin.free();
@@ -1343,10 +1366,7 @@ lj_status lj_step(lj_system* s, double dt, int32_t nsteps) {
     s->launches += ge->kernels;
     if (fused) s->qpar ^= 1;  // the step wrote the next predictor into the other buffer
     if (fused) s->obs_maybe_pending = true;
-    if (s->counter_cap > 0 || s->rdf_acc) {
-      lj_status ast = after_step(s);
-      if (ast) return ast;
-    }
+    after_step_host(s);
   }
   return LJ_OK;
 }
@@ -1621,6 +1641,7 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
   if (!s) return LJ_ERR_INVALID;
   DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  if (s->counter_cap > 0) clear_graphs(s);  // the step graphs hold the counters' launches
   s->counters.clear();
   s->counter_cap = 0;
   s->counter_bins = 0;
@@ -1654,28 +1675,48 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
   s->counter_bins = bins;
   // counting starts only once both buffers exist (counter_cap > 0); on a
   // failure the handle is left with no counters
+  int words[kCtrWords] = {0};
+  words[kCtrNext] = 0;
+  words[kCtrPhase] = 0;
+  words[kCtrEvery] = s->counter_every;
+  words[kCtrCap] = ring_steps;
+  words[kCtrRow] = -1;
   cudaError_t e = s->dcounters.alloc(s->counters.size());
   if (e == cudaSuccess) e = s->counter_ring.alloc((size_t)bins * ring_steps);
+  if (e == cudaSuccess) e = s->counter_state.alloc(kCtrWords);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s->dcounters.p, s->counters.data(), sizeof(CounterDev) * s->counters.size(),
                         cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->counter_state.p, words, sizeof(words), cudaMemcpyHostToDevice, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) {
     s->counters.clear();
     s->counter_bins = 0;
     s->dcounters.free();
     s->counter_ring.free();
+    s->counter_state.free();
   }
   LJ_CUDA(s, e);
   s->counter_cap = ring_steps;
+  clear_graphs(s);  // the step graphs now count
   return LJ_OK;
 }
 
 lj_status lj_counters_set_interval(lj_system* s, int32_t every) {
   if (!s) return LJ_ERR_INVALID;
   if (every < 1) return fail(s, LJ_ERR_INVALID, "the counting interval must be >= 1 step");
+  DeviceGuard device_guard(s->device);
   s->counter_every = every;
   s->counter_phase = 0;
+  if (s->counter_state.p) {
+    // the device's copy, behind the queued steps (phase and interval words)
+    const int words[2] = {0, every};
+    static_assert(kCtrEvery == kCtrPhase + 1, "phase and interval words are adjacent");
+    LJ_CUDA(s, cudaMemcpyAsync(s->counter_state.p + kCtrPhase, words, sizeof(words), cudaMemcpyHostToDevice,
+                               s->stream));
+    LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  }
   return LJ_OK;
 }
 
@@ -1718,6 +1759,7 @@ lj_status lj_rdf_accumulate(lj_system* s, int32_t enable, int32_t mode, int32_t 
   if (!s) return LJ_ERR_INVALID;
   DeviceGuard device_guard(s->device);
   LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  if (s->rdf_acc) clear_graphs(s);  // the step graphs hold the accumulation's launches
   s->rdf_acc = false;
   s->rdf_samples = 0;
   if (!enable) return LJ_OK;
@@ -1743,6 +1785,7 @@ lj_status lj_rdf_accumulate(lj_system* s, int32_t enable, int32_t mode, int32_t 
   h.counts = s->rdf_sum.p;
   s->rdf_args = h;
   s->rdf_acc = true;
+  clear_graphs(s);  // the step graphs now accumulate
   return LJ_OK;
 }
 
