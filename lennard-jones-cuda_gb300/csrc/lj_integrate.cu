@@ -442,64 +442,71 @@ __global__ void k_obs_finalize(StateArgs s) {
 //   slab (type t < 3):  k = (int)((x_t / L) / alpha_step)
 //   cube (type 3):      k = max over axes of #{tl_j <= |x_c - L/2| / 0.5}
 //   velocity (4 .. 6):  k = (int)((|v_c| / vmax) / alpha_step)
-// Per-step bookkeeping of the counters, before k_counters (one CTA): whether
-// this step is counted (every `every`-th step) and into which ring row; that
-// row is cleared here.  st: CounterState words.  On the device, so the
-// counters run inside the captured step graph.
-__global__ void k_counter_prep(int* st, int* ring, int nbins) {
-  __shared__ int row;
-  if (threadIdx.x == 0) {
-    row = -1;
-    if (++st[kCtrPhase] >= st[kCtrEvery]) {
-      st[kCtrPhase] = 0;
-      row = st[kCtrNext];
-      st[kCtrNext] = row + 1 == st[kCtrCap] ? 0 : row + 1;
-    }
-    st[kCtrRow] = row;
-  }
-  __syncthreads();
-  if (row >= 0)
-    for (int b = threadIdx.x; b < nbins; b += blockDim.x) ring[(size_t)row * nbins + b] = 0;
-}
-
-__global__ void k_counters(StateArgs s, const CounterDev* cs, int nc, int nbins, const int* st, int* ring, int n) {
-  const int r = st[kCtrRow];
-  if (r < 0) return;  // not a counted step
-  int* row = ring + (size_t)r * nbins;
+// One launch per step, graph-capturable (everything that changes per step
+// lives in st, the kCtr* words).  Whether the step is counted (every
+// `every`-th step) is read at the start by every CTA; st is written only by
+// the last CTA to finish, after every CTA has taken its ticket.  A counted
+// step: each CTA histograms its particles in shared memory and writes its
+// counts to part[block][bin]; the last CTA sums the blocks' counts into the
+// step's ring row (written whole: no clearing pass) and advances the row.
+__global__ void k_counters(StateArgs s, const CounterDev* cs, int nc, int nbins, int* st, int* ring, int* part,
+                           int n) {
   extern __shared__ int shc[];
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) shc[b] = 0;
-  __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    const double L = s.boxes[0].L;
-    double x[3], v[3];
+  __shared__ bool last;
+  const int phase = st[kCtrPhase] + 1;
+  const bool counted = phase >= st[kCtrEvery];
+  if (counted) {
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) shc[b] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+      const double L = s.boxes[0].L;
+      double x[3], v[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      x[c] = s.x[(size_t)c * s.npad + i];
-      v[c] = s.v[(size_t)c * s.npad + i];
-    }
-    for (int q = 0; q < nc; ++q) {
-      const CounterDev& cd = cs[q];
-      int k;
-      if (cd.type < 3) {
-        k = (int)((x[cd.type] / L) / cd.alpha_step);
-      } else if (cd.type == 3) {
-        k = 0;
-        for (int c = 0; c < 3; ++c) {
-          const double d = fabs(x[c] - 0.5 * L) / 0.5;
-          int kc = 0;
-          while (kc < cd.nalpha && cd.tl[kc] <= d) ++kc;
-          k = kc > k ? kc : k;
-        }
-      } else {
-        k = (int)((fabs(v[cd.type - 4]) / cd.vmax) / cd.alpha_step);
+      for (int c = 0; c < 3; ++c) {
+        x[c] = s.x[(size_t)c * s.npad + i];
+        v[c] = s.v[(size_t)c * s.npad + i];
       }
-      if (k >= 0 && k < cd.nalpha) atomicAdd(&shc[cd.bin0 + k], 1);
+      for (int q = 0; q < nc; ++q) {
+        const CounterDev& cd = cs[q];
+        int k;
+        if (cd.type < 3) {
+          k = (int)((x[cd.type] / L) / cd.alpha_step);
+        } else if (cd.type == 3) {
+          k = 0;
+          for (int c = 0; c < 3; ++c) {
+            const double d = fabs(x[c] - 0.5 * L) / 0.5;
+            int kc = 0;
+            while (kc < cd.nalpha && cd.tl[kc] <= d) ++kc;
+            k = kc > k ? kc : k;
+          }
+        } else {
+          k = (int)((fabs(v[cd.type - 4]) / cd.vmax) / cd.alpha_step);
+        }
+        if (k >= 0 && k < cd.nalpha) atomicAdd(&shc[cd.bin0 + k], 1);
+      }
     }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) part[(size_t)blockIdx.x * nbins + b] = shc[b];
   }
+  __threadfence();
   __syncthreads();
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
-    if (shc[b]) atomicAdd(row + b, shc[b]);
+  if (threadIdx.x == 0) last = atomicAdd(&st[kCtrTicket], 1) == (int)gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int row = st[kCtrNext];
+  if (counted)
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
+      int sum = 0;
+      for (int k = 0; k < (int)gridDim.x; ++k) sum += __ldcg(part + (size_t)k * nbins + b);
+      ring[(size_t)row * nbins + b] = sum;
+    }
+  if (threadIdx.x == 0) {
+    st[kCtrTicket] = 0;
+    st[kCtrPhase] = counted ? 0 : phase;
+    if (counted) st[kCtrNext] = row + 1 == st[kCtrCap] ? 0 : row + 1;
+  }
 }
 
 // |v| histogram (MDSystem.cpp:658-662): b = floor(sqrt(v.v)/step), b < nb.
@@ -731,13 +738,11 @@ cudaError_t launch_predict(const StateArgs& s, int nblocks, int bi, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* state, int* ring, int n,
-                            cudaStream_t st) {
-  k_counter_prep<<<1, 256, 0, st>>>(state, ring, nbins);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  const int threads = 256;
-  k_counters<<<(n + threads - 1) / threads, threads, sizeof(int) * nbins, st>>>(s, cs, nc, nbins, state, ring, n);
+int counters_blocks(int n) { return (n + 255) / 256; }
+
+cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* state, int* ring,
+                            int* part, int n, cudaStream_t st) {
+  k_counters<<<counters_blocks(n), 256, sizeof(int) * nbins, st>>>(s, cs, nc, nbins, state, ring, part, n);
   return cudaGetLastError();
 }
 

@@ -145,14 +145,16 @@ struct CounterDev {
 };
 // Device words of the counters (DevBuf<int> of kCtrWords): next ring row,
 // steps since the last counted one, the interval, the ring's rows, and the
-// row of the current step (-1: not counted).
-enum : int { kCtrNext = 0, kCtrPhase = 1, kCtrEvery = 2, kCtrCap = 3, kCtrRow = 4, kCtrWords = 8 };
-// One step of the counters, two launches (graph-capturable: everything that
-// changes per step lives in `state`): the bookkeeping, which clears the
-// step's ring row when the step is counted, then the histogram of the
-// counters' bin indices over the particles of box 0 added into that row.
-cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* state, int* ring, int n,
-                            cudaStream_t st);
+// per-launch ticket counter (0 between launches).
+enum : int { kCtrNext = 0, kCtrPhase = 1, kCtrEvery = 2, kCtrCap = 3, kCtrTicket = 4, kCtrWords = 8 };
+// One step of the counters in one launch (graph-capturable: everything that
+// changes per step lives in `state`): the histogram of the counters' bin
+// indices over the particles of box 0, per CTA into part (counters_blocks(n)
+// x nbins ints), summed by the last CTA into the step's ring row when the
+// step is counted.
+int counters_blocks(int n);
+cudaError_t launch_counters(const StateArgs& s, const CounterDev* cs, int nc, int nbins, int* state, int* ring,
+                            int* part, int n, cudaStream_t st);
 cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaStream_t st);
 cudaError_t launch_selftest_wait(int* status, cudaStream_t st);
 // Up to three (N,3) interleaved <-> component-major [3][npad] transposes in one launch.

@@ -249,6 +249,7 @@ struct lj_system {
   DevBuf<CounterDev> dcounters;
   DevBuf<int> counter_ring;
   DevBuf<int> counter_state;     // kCtr* words: the device's copy of the bookkeeping below
+  DevBuf<int> counter_part;      // per-CTA counts of the counting launch
   int counter_bins = 0, counter_cap = 0;
   int counter_every = 1;         // count after every counter_every-th step
   long long counter_phase = 0;   // steps since the last counted one
@@ -771,8 +772,8 @@ lj_status flush_observables(lj_system* s) {
 lj_status enqueue_after_step(lj_system* s, const PairArgs* hist, int hist_grid, int* kernels) {
   if (s->counter_cap > 0) {
     LJ_CUDA(s, launch_counters(state_args(s), s->dcounters.p, (int)s->counters.size(), s->counter_bins,
-                               s->counter_state.p, s->counter_ring.p, s->ntotal, s->stream));
-    *kernels += 2;
+                               s->counter_state.p, s->counter_ring.p, s->counter_part.p, s->ntotal, s->stream));
+    *kernels += 1;
   }
   if (s->rdf_acc) {
     StateArgs a = state_args(s);
@@ -786,7 +787,7 @@ lj_status enqueue_after_step(lj_system* s, const PairArgs* hist, int hist_grid, 
 }
 
 // The host's mirror of that bookkeeping, after every launched step: the same
-// counting decision as k_counter_prep, and one more RDF sample.
+// counting decision as k_counters, and one more RDF sample.
 void after_step_host(lj_system* s) {
   if (s->counter_cap > 0 && ++s->counter_phase >= s->counter_every) {
     s->counter_phase = 0;
@@ -1089,6 +1090,7 @@ lj_status lj_destroy(lj_system* s) {
   s->dcounters.free();
   s->counter_ring.free();
   s->counter_state.free();
+  s->counter_part.free();
   s->rdf_sum.free();
   s->qhist.free();
   s->h_cta_tile_begin.free();
@@ -1680,10 +1682,11 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
   words[kCtrPhase] = 0;
   words[kCtrEvery] = s->counter_every;
   words[kCtrCap] = ring_steps;
-  words[kCtrRow] = -1;
+  words[kCtrTicket] = 0;
   cudaError_t e = s->dcounters.alloc(s->counters.size());
   if (e == cudaSuccess) e = s->counter_ring.alloc((size_t)bins * ring_steps);
   if (e == cudaSuccess) e = s->counter_state.alloc(kCtrWords);
+  if (e == cudaSuccess) e = s->counter_part.alloc((size_t)counters_blocks(s->ntotal) * bins);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s->dcounters.p, s->counters.data(), sizeof(CounterDev) * s->counters.size(),
                         cudaMemcpyHostToDevice, s->stream);
@@ -1696,6 +1699,7 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
     s->dcounters.free();
     s->counter_ring.free();
     s->counter_state.free();
+    s->counter_part.free();
   }
   LJ_CUDA(s, e);
   s->counter_cap = ring_steps;
