@@ -439,9 +439,30 @@ __global__ void k_obs_finalize(StateArgs s) {
 // GetNSubsystemBatch / GetNsubVzBatch): per particle and counter, the index
 // of the first alpha whose subsystem contains it; the host turns the
 // histogram into cumulative counts N(alpha_k).
-//   slab (type t < 3):  k = (int)((x_t / L) / alpha_step)
+//   slab (type t < 3):  k = (int)((x_t / L) / alpha_step)   (bin_trunc_div2)
 //   cube (type 3):      k = max over axes of #{tl_j <= |x_c - L/2| / 0.5}
 //   velocity (4 .. 6):  k = (int)((|v_c| / vmax) / alpha_step)
+// (int)((a / b) / c) for b, c > 0: the bin index as the reference forms it
+// (two separately rounded divisions, truncated toward zero), with the
+// divisions skipped where they cannot change the result.  a * inv_bc
+// (inv_bc = 1 / (b c) from the host) is within 1e-15 of that quotient,
+// relatively; where q (1 - 1e-12) and q (1 + 1e-12) truncate to the same
+// integer, so does the reference's quotient.  The divisions (a long FP64
+// sequence each, at 1/64 of the FP32 rate on this part) run only next to a
+// bin edge.
+__device__ __forceinline__ int bin_trunc_div2(double a, double b, double c, double inv_bc) {
+  const double q = a * inv_bc;
+  const int lo = (int)(q * (1.0 - 1e-12)), hi = (int)(q * (1.0 + 1e-12));
+  if (lo == hi) return lo;
+  return (int)((a / b) / c);
+}
+
+// d >= e for non-negative, non-NaN doubles, on their bit patterns (integer
+// pipe): such doubles order like their bits as signed integers.
+__device__ __forceinline__ bool ge_nonneg(double d, double e) {
+  return __double_as_longlong(d) >= __double_as_longlong(e);
+}
+
 // One launch per step, graph-capturable (everything that changes per step
 // lives in st, the kCtr* words).  Whether the step is counted (every
 // `every`-th step) is read at the start by every CTA; st is written only by
@@ -471,17 +492,17 @@ __global__ void k_counters(StateArgs s, const CounterDev* cs, int nc, int nbins,
         const CounterDev& cd = cs[q];
         int k;
         if (cd.type < 3) {
-          k = (int)((x[cd.type] / L) / cd.alpha_step);
+          k = bin_trunc_div2(x[cd.type], L, cd.alpha_step, cd.inv_bc);
         } else if (cd.type == 3) {
           k = 0;
           for (int c = 0; c < 3; ++c) {
-            const double d = fabs(x[c] - 0.5 * L) / 0.5;
+            const double d = fabs(x[c] - 0.5 * L) * 2.0;  // = / 0.5, exactly
             int kc = 0;
-            while (kc < cd.nalpha && cd.tl[kc] <= d) ++kc;
+            while (kc < cd.nalpha && ge_nonneg(d, cd.tl[kc])) ++kc;
             k = kc > k ? kc : k;
           }
         } else {
-          k = (int)((fabs(v[cd.type - 4]) / cd.vmax) / cd.alpha_step);
+          k = bin_trunc_div2(fabs(v[cd.type - 4]), cd.vmax, cd.alpha_step, cd.inv_bc);
         }
         if (k >= 0 && k < cd.nalpha) atomicAdd(&shc[cd.bin0 + k], 1);
       }

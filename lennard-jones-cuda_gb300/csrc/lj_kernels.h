@@ -141,6 +141,7 @@ struct CounterDev {
   int pad;
   double alpha_step;
   double vmax;
+  double inv_bc;                 // 1 / (L alpha_step) (types 0-2) or 1 / (vmax alpha_step) (types 4-6)
   double tl[kMaxCounterAlphas];  // type 3: cube sides L alpha_k^(1/3)
 };
 // Device words of the counters (DevBuf<int> of kCtrWords): next ring row,

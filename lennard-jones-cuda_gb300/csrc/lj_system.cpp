@@ -1668,6 +1668,7 @@ lj_status lj_counters_configure(lj_system* s, const lj_counter* counters, int32_
     d.bin0 = bins;
     d.alpha_step = c.alpha_step;
     d.vmax = c.vmax;
+    d.inv_bc = 1.0 / ((c.type >= 4 ? c.vmax : L) * c.alpha_step);
     // cube sides from the accumulated alphas, as the reference's loop forms them
     double alpha = c.alpha_step;
     for (int k = 0; k < c.nalpha; ++k, alpha += c.alpha_step) d.tl[k] = L * std::pow(alpha, 1. / 3.);
