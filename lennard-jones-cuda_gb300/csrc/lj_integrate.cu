@@ -595,18 +595,41 @@ __global__ void k_unpack(const double* __restrict__ in, double* __restrict__ out
 // link) and gathers it from the device array.  With a mailbox, the row after
 // the arrays copies the status words and the scalar block into the handle's
 // page-locked mirrors (destinations may be mapped host memory: the host reads
-// them after one synchronisation, with no copy operation queued).
-__global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb) {
+// them after one synchronisation, with no copy operation queued); with
+// mb.finalize it first computes the observables a fused TVN step left
+// pending, as k_obs_finalize would, one CTA per box (one launch fewer per
+// read-back after a step).
+__global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb, StateArgs s) {
   if ((int)blockIdx.y == count) {
-    if (blockIdx.x != 0) return;
+    const int nb = mb.finalize ? s.nsys : 1;
+    if ((int)blockIdx.x >= nb) return;
+    if (mb.finalize) {
+      // The observables k_obs_finalize would compute (box blockIdx.x), then
+      // that box's scalar block; the status words follow once every box is
+      // done, since a box's observables may flag the status.
+      __shared__ double sh[3 * 32];
+      __shared__ int last;
+      pending_observables(s, blockIdx.x, nb, sh);
+      const int wb = mb.sc_nwords / nb;
+      for (int k = threadIdx.x; k < wb; k += blockDim.x) mb.sc_out[blockIdx.x * wb + k] = mb.sc[blockIdx.x * wb + k];
+      if (nb > 1) {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) last = atomicAdd(mb.ticket, 1) == nb - 1;
+        __syncthreads();
+        if (!last) return;
+        if (threadIdx.x == 0) *mb.ticket = 0;
+      }
+    } else {
+      for (int k = threadIdx.x; k < mb.sc_nwords; k += blockDim.x) mb.sc_out[k] = mb.sc[k];
+    }
     if (threadIdx.x == 0) {
-      mb.words_out[0] = *mb.status;
+      mb.words_out[0] = *(volatile const int*)mb.status;
       if (mb.bad) {
         mb.words_out[1] = *mb.bad;
         *mb.bad = 0x7f7f7f7f;  // read: ready for the next upload's check
       }
     }
-    for (int k = threadIdx.x; k < mb.sc_nwords; k += blockDim.x) mb.sc_out[k] = mb.sc[k];
     return;
   }
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -687,10 +710,13 @@ cudaError_t launch_unpack(const double* in, double* out, int n, int npad, cudaSt
   return cudaGetLastError();
 }
 
-cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, cudaStream_t st) {
+cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, const StateArgs& s,
+                              cudaStream_t st) {
   const int rows = count + (mb ? 1 : 0);
   if (rows <= 0) return cudaSuccess;
-  k_pack_multi<<<dim3((3 * n + 255) / 256, rows), 256, 0, st>>>(a, count, n, npad, mb ? *mb : Mailbox{});
+  int gx = (3 * n + 255) / 256;
+  if (mb && mb->finalize && gx < s.nsys) gx = s.nsys;
+  k_pack_multi<<<dim3(gx, rows), 256, 0, st>>>(a, count, n, npad, mb ? *mb : Mailbox{}, s);
   return cudaGetLastError();
 }
 

@@ -173,8 +173,12 @@ struct Mailbox {
   const int* sc;
   int* sc_out;
   int sc_nwords;
+  int finalize;  // != 0: compute the observables the last fused TVN step left pending first (one CTA per box)
+  int* ticket;   // finalize with several boxes: the last box's CTA copies the status words (0 between launches)
 };
-cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, cudaStream_t st);
+// `s` is read only with mb->finalize.
+cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, const StateArgs& s,
+                              cudaStream_t st);
 // Upload of (N,3) positions / velocities (either may be NULL; either may be
 // mapped host memory), in two launches.  Stage: every value checked (*bad
 // receives the lowest index of a non-finite value, velocities after the 3n

@@ -221,6 +221,7 @@ struct lj_system {
   DevBuf<double> x, v, f, tf, e, w;
   DevBuf<double> stage;          // 3 x (N,3) interleaved host-format arrays: positions, velocities, forces
   DevBuf<int> bad;               // lowest index of a non-finite uploaded value (INT_MAX: none)
+  DevBuf<int> mb_ticket;         // read-back that finalizes several boxes: boxes done (0 between launches)
   PinnedBuf<int> h_words;        // [0] status, [1] bad index: read back after one synchronisation
   bool upload_check_pending = false;  // lj_set_state_async queued a finiteness check not yet read back
   bool bad_clean = false;             // s->bad holds 0x7f7f7f7f (reset by the read-back of a check)
@@ -283,6 +284,10 @@ struct lj_system {
   long long launches = 0;
   std::string err;
 };
+
+extern "C" {
+static lj_status enqueue_read(lj_system* s, double* pos, double* vel, double* force, bool scalars);
+}
 
 namespace {
 
@@ -824,6 +829,7 @@ lj_status finish_status(lj_system* s) {
     // A failed launch may leave the fused-step counters mid-count.
     if (s->blk_cnt.p) LJ_CUDA(s, cudaMemsetAsync(s->blk_cnt.p, 0, sizeof(int) * s->blk_cnt.n, s->stream));
     if (s->glob_cnt.p) LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n, s->stream));
+    if (s->mb_ticket.p) LJ_CUDA(s, cudaMemsetAsync(s->mb_ticket.p, 0, sizeof(int), s->stream));
     s->pred_ready = false;
     if (st & LJ_DEVFLAG_TIMEOUT)
       return fail(s, LJ_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the results of that launch are void");
@@ -858,6 +864,7 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, s->tf.alloc(n3));
   LJ_CUDA(s, s->stage.alloc(4 * n3));  // uploads: 2 (N,3) + 2 component-major arrays; reads: 3 (N,3)
   LJ_CUDA(s, s->bad.alloc(1));
+  LJ_CUDA(s, s->mb_ticket.alloc(1));
   LJ_CUDA(s, s->h_words.alloc(2));
   LJ_CUDA(s, s->h_sc.alloc(s->nsys));
   LJ_CUDA(s, s->e.alloc(s->npad));
@@ -878,6 +885,7 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, cudaMemsetAsync(s->xd.p, 0, sizeof(double4_32a) * s->npad, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->sc.p, 0, sizeof(DevScalars) * s->nsys, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->status.p, 0, sizeof(int), s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->mb_ticket.p, 0, sizeof(int), s->stream));
   return LJ_OK;
 }
 
@@ -896,6 +904,12 @@ lj_status upload_xyz(lj_system* s, const double* host, double* dev) {
 // Per-box scalars into the pinned mirror h_sc (check_status semantics: one
 // synchronisation, device status reported).
 lj_status fetch_scalars(lj_system* s) {
+  if (s->h_words.dev && s->h_sc.dev) {
+    // one launch: pending observables, scalar block and status words
+    lj_status st = enqueue_read(s, nullptr, nullptr, nullptr, true);
+    if (st) return st;
+    return finish_status(s);
+  }
   lj_status st = flush_observables(s);
   if (st) return st;
   LJ_CUDA(s, cudaMemcpyAsync(s->h_sc.p, s->sc.p, sizeof(DevScalars) * s->nsys, cudaMemcpyDeviceToHost, s->stream));
@@ -1258,9 +1272,17 @@ static lj_status enqueue_read(lj_system* s, double* pos, double* vel, double* fo
       mb.sc = reinterpret_cast<const int*>(s->sc.p);
       mb.sc_out = static_cast<int*>(s->h_sc.dev);
       mb.sc_nwords = (int)(sizeof(DevScalars) * s->nsys / sizeof(int));
+      // the pending observables are computed by the same launch
+      mb.finalize = s->obs_maybe_pending ? 1 : 0;
+      mb.ticket = s->mb_ticket.p;
+      s->obs_maybe_pending = false;
     }
   }
-  LJ_CUDA(s, launch_pack_multi(xa, na, s->ntotal, s->npad, mailbox ? &mb : nullptr, s->stream));
+  if (scalars && !mailbox) {
+    lj_status st = flush_observables(s);
+    if (st) return st;
+  }
+  LJ_CUDA(s, launch_pack_multi(xa, na, s->ntotal, s->npad, mailbox ? &mb : nullptr, state_args(s), s->stream));
   if (na > 0 || mailbox) s->launches += 1;
   for (int k = 0; k < na; ++k)
     if (host[k])
@@ -1289,8 +1311,8 @@ lj_status lj_get_state(lj_system* s, double* pos, double* vel, double* force) {
 lj_status lj_get_state_observables(lj_system* s, double* pos, double* vel, double* force, lj_observables* out) {
   if (!s) return LJ_ERR_INVALID;
   DeviceGuard device_guard(s->device);
-  lj_status st = flush_observables(s);
-  if (st) return st;
+  lj_status st;
+  if (!out && (st = flush_observables(s))) return st;
   if ((st = enqueue_read(s, pos, vel, force, out != nullptr))) return st;
   if ((st = finish_status(s))) return st;
   if (out) fill_obs(s->h_sc.p[0], out);
