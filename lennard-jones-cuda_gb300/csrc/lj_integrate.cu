@@ -645,6 +645,9 @@ __global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb
 // written component-major into the staging buffer.
 __global__ void k_upload_stage(const double* __restrict__ pos, const double* __restrict__ vel, int n, int npad,
                                double* __restrict__ spos, double* __restrict__ svel, int na, int* bad) {
+  // k_upload_commit, launched as a programmatic dependent, may be scheduled
+  // from here on: it waits for this grid's completion before reading.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const double* src = blockIdx.y == 0 ? pos : vel;
   if (!src || k >= 3 * n) return;
@@ -661,24 +664,40 @@ __global__ void k_upload_stage(const double* __restrict__ pos, const double* __r
 // k_predict does, so the first step after an upload needs no predictor launch.
 __global__ void k_upload_commit(StateArgs s, const double* __restrict__ spos, const double* __restrict__ svel,
                                 const int* bad, int predict) {
+  // Launched as a programmatic dependent of k_upload_stage: what the stage
+  // does not write (block table, state, forces) is loaded before waiting for
+  // its grid to complete.
   const BlockInfo bi = s.blocks[blockIdx.x];
-  if ((int)threadIdx.x >= bi.n_i) return;
-  const int p = bi.p0 + bi.i0 + threadIdx.x;
-  const bool ok = *bad == 0x7f7f7f7f;
-  double x[3], v[3];
+  const bool valid = (int)threadIdx.x < bi.n_i;
+  const int p = bi.p0 + bi.i0 + (valid ? (int)threadIdx.x : 0);
+  double x[3], v[3], f[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const size_t k = (size_t)c * s.npad + p;
-    x[c] = (ok && spos) ? spos[k] : s.x[k];
-    v[c] = (ok && svel) ? svel[k] : s.v[k];
-    if (ok && spos) s.x[k] = x[c];
-    if (ok && svel) s.v[k] = v[c];
+    x[c] = s.x[k];
+    v[c] = s.v[k];
+    f[c] = predict ? s.f[k] : 0.0;
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (!valid) return;
+  const bool ok = *bad == 0x7f7f7f7f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = (size_t)c * s.npad + p;
+    if (ok && spos) {
+      x[c] = spos[k];
+      s.x[k] = x[c];
+    }
+    if (ok && svel) {
+      v[c] = svel[k];
+      s.v[k] = v[c];
+    }
   }
   if (!predict) return;
   const BoxArgs box = s.boxes[bi.sys];
   double xp[3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) xp[c] = drift_pos(box, x[c], v[c], s.f[(size_t)c * s.npad + p]);
+  for (int c = 0; c < 3; ++c) xp[c] = drift_pos(box, x[c], v[c], f[c]);
   s.q[p] = shadow_of(s.sc[bi.sys], xp[0], xp[1], xp[2]);
 }
 
@@ -730,8 +749,18 @@ cudaError_t launch_upload_stage(const double* pos, const double* vel, int n, int
 
 cudaError_t launch_upload_commit(const StateArgs& s, int nblocks, int bi, const double* spos, const double* svel,
                                  const int* bad, bool predict, cudaStream_t st) {
-  k_upload_commit<<<nblocks, bi, 0, st>>>(s, spos, svel, bad, predict ? 1 : 0);
-  return cudaGetLastError();
+  // programmatic dependent of the stage launch queued just before it
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(bi);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_upload_commit, s, spos, svel, bad, predict ? 1 : 0);
 }
 
 cudaError_t launch_drift_mode(const StateArgs& s, int nblocks, int bi, int mode, cudaStream_t st) {
