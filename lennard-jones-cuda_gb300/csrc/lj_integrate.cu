@@ -598,44 +598,63 @@ __global__ void k_unpack(const double* __restrict__ in, double* __restrict__ out
 // them after one synchronisation, with no copy operation queued); with
 // mb.finalize it first computes the observables a fused TVN step left
 // pending, as k_obs_finalize would, one CTA per box (one launch fewer per
-// read-back after a step).
+// read-back after a step).  With mb.seq the last CTA to finish writes a
+// completion word for the host to wait on.
+__device__ __forceinline__ void mailbox_row(const Mailbox& mb, const StateArgs& s) {
+  const int nb = mb.finalize ? s.nsys : 1;
+  if ((int)blockIdx.x >= nb) return;
+  if (mb.finalize) {
+    // The observables k_obs_finalize would compute (box blockIdx.x), then
+    // that box's scalar block; the status words follow once every box is
+    // done, since a box's observables may flag the status.
+    __shared__ double sh[3 * 32];
+    __shared__ int last;
+    pending_observables(s, blockIdx.x, nb, sh);
+    const int wb = mb.sc_nwords / nb;
+    for (int k = threadIdx.x; k < wb; k += blockDim.x) mb.sc_out[blockIdx.x * wb + k] = mb.sc[blockIdx.x * wb + k];
+    if (nb > 1) {
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) last = atomicAdd(mb.ticket, 1) == nb - 1;
+      __syncthreads();
+      if (!last) return;
+      if (threadIdx.x == 0) *mb.ticket = 0;
+    }
+  } else {
+    for (int k = threadIdx.x; k < mb.sc_nwords; k += blockDim.x) mb.sc_out[k] = mb.sc[k];
+  }
+  if (threadIdx.x == 0) {
+    mb.words_out[0] = *(volatile const int*)mb.status;
+    if (mb.bad) {
+      mb.words_out[1] = *mb.bad;
+      *mb.bad = 0x7f7f7f7f;  // read: ready for the next upload's check
+    }
+  }
+}
+
 __global__ void k_pack_multi(XyzArrays a, int count, int n, int npad, Mailbox mb, StateArgs s) {
   if ((int)blockIdx.y == count) {
-    const int nb = mb.finalize ? s.nsys : 1;
-    if ((int)blockIdx.x >= nb) return;
-    if (mb.finalize) {
-      // The observables k_obs_finalize would compute (box blockIdx.x), then
-      // that box's scalar block; the status words follow once every box is
-      // done, since a box's observables may flag the status.
-      __shared__ double sh[3 * 32];
-      __shared__ int last;
-      pending_observables(s, blockIdx.x, nb, sh);
-      const int wb = mb.sc_nwords / nb;
-      for (int k = threadIdx.x; k < wb; k += blockDim.x) mb.sc_out[blockIdx.x * wb + k] = mb.sc[blockIdx.x * wb + k];
-      if (nb > 1) {
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) last = atomicAdd(mb.ticket, 1) == nb - 1;
-        __syncthreads();
-        if (!last) return;
-        if (threadIdx.x == 0) *mb.ticket = 0;
-      }
-    } else {
-      for (int k = threadIdx.x; k < mb.sc_nwords; k += blockDim.x) mb.sc_out[k] = mb.sc[k];
+    mailbox_row(mb, s);
+  } else {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < 3 * n) {
+      const int i = k / 3, c = k - 3 * i;
+      a.dst[blockIdx.y][k] = a.src[blockIdx.y][(size_t)c * npad + i];
     }
-    if (threadIdx.x == 0) {
-      mb.words_out[0] = *(volatile const int*)mb.status;
-      if (mb.bad) {
-        mb.words_out[1] = *mb.bad;
-        *mb.bad = 0x7f7f7f7f;  // read: ready for the next upload's check
-      }
-    }
-    return;
   }
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= 3 * n) return;
-  const int i = k / 3, c = k - 3 * i;
-  a.dst[blockIdx.y][k] = a.src[blockIdx.y][(size_t)c * npad + i];
+  if (mb.seq) {
+    // every thread's stores before its CTA's count (a fence orders only the
+    // calling thread's own stores)
+    __threadfence_system();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (atomicAdd(mb.grid_ticket, 1) == (int)(gridDim.x * gridDim.y) - 1) {
+        *mb.grid_ticket = 0;
+        __threadfence_system();
+        *(volatile int*)(mb.words_out + 2) = mb.seq;
+      }
+    }
+  }
 }
 
 // First half of an upload: (N,3) positions (blockIdx.y = 0) and velocities

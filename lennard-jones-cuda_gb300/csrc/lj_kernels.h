@@ -175,6 +175,11 @@ struct Mailbox {
   int sc_nwords;
   int finalize;  // != 0: compute the observables the last fused TVN step left pending first (one CTA per box)
   int* ticket;   // finalize with several boxes: the last box's CTA copies the status words (0 between launches)
+  // seq != 0: the launch's last CTA writes seq into words_out[2] once every
+  // store of the launch is visible to the host (grid_ticket: CTAs done, 0
+  // between launches), so the host can wait on that word alone.
+  int* grid_ticket;
+  int seq;
 };
 // `s` is read only with mb->finalize.
 cudaError_t launch_pack_multi(const XyzArrays& a, int count, int n, int npad, const Mailbox* mb, const StateArgs& s,

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -221,8 +222,11 @@ struct lj_system {
   DevBuf<double> x, v, f, tf, e, w;
   DevBuf<double> stage;          // 3 x (N,3) interleaved host-format arrays: positions, velocities, forces
   DevBuf<int> bad;               // lowest index of a non-finite uploaded value (INT_MAX: none)
-  DevBuf<int> mb_ticket;         // read-back that finalizes several boxes: boxes done (0 between launches)
-  PinnedBuf<int> h_words;        // [0] status, [1] bad index: read back after one synchronisation
+  DevBuf<int> mb_ticket;         // read-back launch: [0] boxes finalized, [1] CTAs done (0 between launches)
+  PinnedBuf<int> h_words;        // [0] status, [1] bad index: read back after one synchronisation;
+                                 // [2] completion word of the last read-back launch
+  int mb_seq = 0;                // last completion word queued
+  int mb_wait = 0;               // completion word finish_status waits for (0: synchronise the stream)
   bool upload_check_pending = false;  // lj_set_state_async queued a finiteness check not yet read back
   bool bad_clean = false;             // s->bad holds 0x7f7f7f7f (reset by the read-back of a check)
   PinnedBuf<DevScalars> h_sc;    // per-box scalars read back
@@ -812,11 +816,30 @@ lj_status enqueue_status_read(lj_system* s) {
   return LJ_OK;
 }
 
-// Synchronises the handle's stream and reports what the status words queued
-// for h_words say.
+// Waits for the read-back launch's completion word when one was queued (it
+// is written after every store of that launch, the last work queued; a word
+// that does not come within 20 ms -- a long run of steps before it, or a
+// failed launch -- falls back to synchronising the stream, which also
+// reports errors), else synchronises the stream; then reports what the
+// status words queued for h_words say.
+static bool wait_completion_word(lj_system* s) {
+  const int want = s->mb_wait;
+  s->mb_wait = 0;
+  if (!want) return false;
+  const volatile int* w = s->h_words.p + 2;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (unsigned it = 1;; ++it) {
+    if (*w == want) {
+      std::atomic_thread_fence(std::memory_order_acquire);
+      return true;
+    }
+    if ((it & 255u) == 0 && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(20)) return false;
+  }
+}
+
 lj_status finish_status(lj_system* s) {
   const bool upload = s->upload_check_pending;
-  LJ_CUDA(s, cudaStreamSynchronize(s->stream));
+  if (!wait_completion_word(s)) LJ_CUDA(s, cudaStreamSynchronize(s->stream));
   s->upload_check_pending = false;
   if (upload && s->h_words.p[1] != 0x7f7f7f7f)
     return fail(s, LJ_ERR_INVALID, "an array queued by lj_set_state_async held a non-finite value (element %d of "
@@ -829,7 +852,7 @@ lj_status finish_status(lj_system* s) {
     // A failed launch may leave the fused-step counters mid-count.
     if (s->blk_cnt.p) LJ_CUDA(s, cudaMemsetAsync(s->blk_cnt.p, 0, sizeof(int) * s->blk_cnt.n, s->stream));
     if (s->glob_cnt.p) LJ_CUDA(s, cudaMemsetAsync(s->glob_cnt.p, 0, sizeof(int) * s->glob_cnt.n, s->stream));
-    if (s->mb_ticket.p) LJ_CUDA(s, cudaMemsetAsync(s->mb_ticket.p, 0, sizeof(int), s->stream));
+    if (s->mb_ticket.p) LJ_CUDA(s, cudaMemsetAsync(s->mb_ticket.p, 0, 2 * sizeof(int), s->stream));
     s->pred_ready = false;
     if (st & LJ_DEVFLAG_TIMEOUT)
       return fail(s, LJ_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the results of that launch are void");
@@ -864,8 +887,8 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, s->tf.alloc(n3));
   LJ_CUDA(s, s->stage.alloc(4 * n3));  // uploads: 2 (N,3) + 2 component-major arrays; reads: 3 (N,3)
   LJ_CUDA(s, s->bad.alloc(1));
-  LJ_CUDA(s, s->mb_ticket.alloc(1));
-  LJ_CUDA(s, s->h_words.alloc(2));
+  LJ_CUDA(s, s->mb_ticket.alloc(2));
+  LJ_CUDA(s, s->h_words.alloc(3));
   LJ_CUDA(s, s->h_sc.alloc(s->nsys));
   LJ_CUDA(s, s->e.alloc(s->npad));
   LJ_CUDA(s, s->w.alloc(s->npad));
@@ -885,7 +908,7 @@ lj_status alloc_state(lj_system* s) {
   LJ_CUDA(s, cudaMemsetAsync(s->xd.p, 0, sizeof(double4_32a) * s->npad, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->sc.p, 0, sizeof(DevScalars) * s->nsys, s->stream));
   LJ_CUDA(s, cudaMemsetAsync(s->status.p, 0, sizeof(int), s->stream));
-  LJ_CUDA(s, cudaMemsetAsync(s->mb_ticket.p, 0, sizeof(int), s->stream));
+  LJ_CUDA(s, cudaMemsetAsync(s->mb_ticket.p, 0, 2 * sizeof(int), s->stream));
   return LJ_OK;
 }
 
@@ -1277,6 +1300,18 @@ static lj_status enqueue_read(lj_system* s, double* pos, double* vel, double* fo
       mb.ticket = s->mb_ticket.p;
       s->obs_maybe_pending = false;
     }
+    // nothing is queued behind this launch (every destination is mapped):
+    // the host may wait on its completion word alone
+    bool staged = false;
+    for (int k = 0; k < na; ++k) staged |= host[k] != nullptr;
+    if (!staged) {
+      s->mb_seq = s->mb_seq == INT32_MAX ? 1 : s->mb_seq + 1;
+      mb.seq = s->mb_seq;
+      mb.grid_ticket = s->mb_ticket.p + 1;
+      // cleared by the host before the launch is queued: page-locked memory
+      // comes back from the allocator holding what an earlier handle left
+      *(volatile int*)(s->h_words.p + 2) = 0;
+    }
   }
   if (scalars && !mailbox) {
     lj_status st = flush_observables(s);
@@ -1284,6 +1319,7 @@ static lj_status enqueue_read(lj_system* s, double* pos, double* vel, double* fo
   }
   LJ_CUDA(s, launch_pack_multi(xa, na, s->ntotal, s->npad, mailbox ? &mb : nullptr, state_args(s), s->stream));
   if (na > 0 || mailbox) s->launches += 1;
+  s->mb_wait = mb.seq;
   for (int k = 0; k < na; ++k)
     if (host[k])
       LJ_CUDA(s, cudaMemcpyAsync(host[k], xa.dst[k], sizeof(double) * n3, cudaMemcpyDeviceToHost, s->stream));
