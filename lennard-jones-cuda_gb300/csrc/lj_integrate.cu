@@ -355,7 +355,8 @@ __global__ void k_predict(StateArgs s) {
 
 // Close of a fused TVN step (MDSystem.cpp:469-506, :578-579).  The pair
 // kernel's epilogue left F_{n+1} in s.tf (s.f still holds F_n), e and w, and
-// chi of every box.  Per particle: x_{n+1} = drift_pos(x_n, v_n, F_n),
+// each block's sum of the half-kicked velocities' squares; chi of the box is
+// formed here from those.  Per particle: x_{n+1} = drift_pos(x_n, v_n, F_n),
 // tF = F_n/2 + F_{n+1}/2, v = (2 chi - 1) v + chi dt tF, boundaries,
 // F <- F_{n+1}, the next step's predictor, and block partials K, V, W.
 // The observables of the step (sums over blocks, averages, record) are left
@@ -385,7 +386,23 @@ __global__ void k_tvn_close(StateArgs s) {
   }
   asm volatile("griddepcontrol.wait;" ::: "memory");
   DevScalars& sc = s.sc[bi.sys];
-  const double chi = sc.chi;
+  // chi of the box (MDSystem.cpp:498-499) from its blocks' sums of the
+  // half-kicked velocities' squares (slot 3, written by the pair kernel's
+  // block epilogues): every CTA of the box forms the same sum in the same
+  // order (as k_tvn_finish does), so no CTA of the pair kernel has to wait
+  // for the box's last block to compute it.
+  __shared__ double chi_sh, tkin_sh;
+  {
+    const int b0 = s.sys_block_first[bi.sys], b1 = s.sys_block_first[bi.sys + 1];
+    const double tv2 = box_sum(s, b0, b1, 3, sh);
+    if (tid == 0) {
+      double Tkin;
+      chi_sh = tvn_chi(box, tv2, &Tkin);
+      tkin_sh = Tkin;
+    }
+    __syncthreads();
+  }
+  const double chi = chi_sh;
   // chi dt tF with tF = (F_n + F_{n+1}) / 2 formed as (chi dt / 2)(F_n + F_{n+1}):
   // the same bits (the halvings are exact), one FP64 operation fewer
   const double a1 = 2. * chi - 1., b1h = 0.5 * (chi * box.dt);
@@ -422,7 +439,9 @@ __global__ void k_tvn_close(StateArgs s) {
     s.blk_part[(size_t)B * 8 + 1] = 0.5 * part[1];
     s.blk_part[(size_t)B * 8 + 2] = part[2];
     if (B == s.sys_block_first[bi.sys]) {
-      sc.Tkin_rec = sc.Tkin;
+      sc.Tkin = tkin_sh;
+      sc.Tkin_rec = tkin_sh;
+      sc.chi = chi;
       sc.obs_slot = 0;
       sc.obs_pending = MODE_TVN;
     }

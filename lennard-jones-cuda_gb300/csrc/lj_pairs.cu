@@ -428,31 +428,32 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           __threadfence();
           fused_block_step<EPI>(st, B, shd);
           __syncthreads();
-          // Last block of its box?  That CTA finishes the box: EVN marks its
-          // observables pending (summed later by pending_observables), TVN
-          // computes its chi.  Boxes finish independently, so a batch of
-          // many boxes has no serial stage at the end of the grid.
-          const int sys = bi.sys;
-          if (tid == 0) {
-            st.blk_cnt[B] = 0;
-            __threadfence();
-            const int nb_box = st.sys_block_first[sys + 1] - st.sys_block_first[sys];
-            sflag = (atomicAdd(st.glob_cnt + 4 + sys, 1) == nb_box - 1);
-          }
-          __syncthreads();
-          if (sflag) {
-            __threadfence();
-            if (EPI == MODE_EVN) {
+          if (EPI == MODE_TVN) {
+            // chi is formed by k_tvn_close from the blocks' sums
+            if (tid == 0) st.blk_cnt[B] = 0;
+          } else {
+            // Last block of its box?  That CTA marks the box's observables
+            // pending (summed later by pending_observables).  Boxes finish
+            // independently, so a batch of many boxes has no serial stage at
+            // the end of the grid.
+            const int sys = bi.sys;
+            if (tid == 0) {
+              st.blk_cnt[B] = 0;
+              __threadfence();
+              const int nb_box = st.sys_block_first[sys + 1] - st.sys_block_first[sys];
+              sflag = (atomicAdd(st.glob_cnt + 4 + sys, 1) == nb_box - 1);
+            }
+            __syncthreads();
+            if (sflag) {
+              __threadfence();
               if (tid == 0) {
                 st.sc[sys].obs_slot = st.obs_slot;
                 st.sc[sys].obs_pending = MODE_EVN;
+                st.glob_cnt[4 + sys] = 0;
               }
-            } else {
-              tvn_chi_box(st, sys, shd);
             }
-            if (tid == 0) st.glob_cnt[4 + sys] = 0;
+            __syncthreads();
           }
-          __syncthreads();
         }
       }
       if (block_end && !last) {

@@ -185,20 +185,6 @@ static __device__ __noinline__ void pending_observables(const StateArgs& s, int 
   }
 }
 
-// TVN scale of box `sys` (MDSystem.cpp:498-499) from the half-kicked
-// velocities' block sums (slot 3).  Block-wide call; thread 0 writes.
-__device__ __forceinline__ void tvn_chi_box(const StateArgs& s, int sys, double* sh) {
-  const BoxArgs box = s.boxes[sys];
-  const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
-  const double tv2 = box_sum(s, b0, b1, 3, sh);
-  if (threadIdx.x == 0) {
-    double Tkin;
-    const double chi = tvn_chi(box, tv2, &Tkin);
-    s.sc[sys].Tkin = Tkin;
-    s.sc[sys].chi = chi;
-  }
-}
-
 // Sum of a particle's pair-kernel segments (5 values each).  The partials are
 // FP32 values carrying TwoSum-compensated sums; they are added here in FP32
 // TwoSum too (exact up to the low word's rounding) and converted to FP64 once,
