@@ -369,7 +369,7 @@ __global__ void k_tvn_close(StateArgs s) {
   // Launched as a programmatic dependent of the pair kernel: the CTAs start
   // while the pair grid drains.  What the pair kernel does not write (the
   // block table, the box, x, v and F_n) is loaded before waiting for its
-  // writes (F_{n+1} in tf, e, w, chi) to become visible.
+  // writes (F_{n+1} in tf, e, w, the blocks' sums) to become visible.
   const int B = blockIdx.x;
   const BlockInfo bi = s.blocks[B];
   const int tid = threadIdx.x;
@@ -384,8 +384,18 @@ __global__ void k_tvn_close(StateArgs s) {
     vn[c] = s.v[k];
     fn[c] = s.f[k];
   }
+  const int b0 = s.sys_block_first[bi.sys], b1 = s.sys_block_first[bi.sys + 1];
   asm volatile("griddepcontrol.wait;" ::: "memory");
   DevScalars& sc = s.sc[bi.sys];
+  // The pair kernel's results for this particle, loaded before chi's sum so
+  // that both wait on memory together.
+  double f1[3], ep = 0.0, wp = 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) f1[c] = s.tf[(size_t)c * s.npad + p];
+  if (valid) {
+    ep = s.e[p];
+    wp = s.w[p];
+  }
   // chi of the box (MDSystem.cpp:498-499) from its blocks' sums of the
   // half-kicked velocities' squares (slot 3, written by the pair kernel's
   // block epilogues): every CTA of the box forms the same sum in the same
@@ -393,7 +403,6 @@ __global__ void k_tvn_close(StateArgs s) {
   // for the box's last block to compute it.
   __shared__ double chi_sh, tkin_sh;
   {
-    const int b0 = s.sys_block_first[bi.sys], b1 = s.sys_block_first[bi.sys + 1];
     const double tv2 = box_sum(s, b0, b1, 3, sh);
     if (tid == 0) {
       double Tkin;
@@ -408,11 +417,9 @@ __global__ void k_tvn_close(StateArgs s) {
   const double a1 = 2. * chi - 1., b1h = 0.5 * (chi * box.dt);
   double part[3] = {0.0, 0.0, 0.0};
   if (valid) {
-    double x[3], v[3], f1[3];
+    double x[3], v[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const size_t k = (size_t)c * s.npad + p;
-      f1[c] = s.tf[k];
       x[c] = drift_pos(box, xn[c], vn[c], fn[c]);
       v[c] = fma(a1, vn[c], b1h * (fn[c] + f1[c]));
     }
@@ -429,8 +436,8 @@ __global__ void k_tvn_close(StateArgs s) {
     check_wall_frame(s, box.bc, sc, xp[0], xp[1], xp[2]);
     s.q_next[p] = shadow_of_bc(sc, box.bc, xp[0], xp[1], xp[2]);
     part[0] = fma(v[0], v[0], fma(v[1], v[1], v[2] * v[2]));  // K and V shares, halved once per block below
-    part[1] = s.e[p];
-    part[2] = s.w[p];
+    part[1] = ep;
+    part[2] = wp;
   }
   block_sum<3>(part, sh);
   if (tid == 0) {
