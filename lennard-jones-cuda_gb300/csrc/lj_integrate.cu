@@ -298,7 +298,6 @@ __global__ void k_tvn_finish(StateArgs s) {
     chi_sh = chi;
     if (B == b0) {
       s.sc[bi.sys].Tkin = Tkin;
-      s.sc[bi.sys].Tkin_rec = Tkin;
       s.sc[bi.sys].chi = chi;
     }
   }
@@ -446,11 +445,12 @@ __global__ void k_tvn_close(StateArgs s) {
     s.blk_part[(size_t)B * 8 + 1] = 0.5 * part[1];
     s.blk_part[(size_t)B * 8 + 2] = part[2];
     if (B == s.sys_block_first[bi.sys]) {
+      const int par = s.ticket - 2;  // this step's parity
       sc.Tkin = tkin_sh;
-      sc.Tkin_rec = tkin_sh;
+      sc.Tkin_rec[par] = tkin_sh;
       sc.chi = chi;
-      sc.obs_slot = 0;
-      sc.obs_pending = MODE_TVN;
+      sc.obs_slot[par] = 0;
+      sc.obs_pending[par] = MODE_TVN;
     }
   }
 }
@@ -458,7 +458,7 @@ __global__ void k_tvn_close(StateArgs s) {
 // Observables left pending by the last fused TVN step (one CTA per box).
 __global__ void k_obs_finalize(StateArgs s) {
   __shared__ double sh[3 * 32];
-  pending_observables(s, blockIdx.x, gridDim.x, sh);
+  pending_observables_all(s, blockIdx.x, gridDim.x, sh);
 }
 
 // Subsystem counters of the fluctuation task (run-fluctuations-aux.h:124-273,
@@ -635,7 +635,7 @@ __device__ __forceinline__ void mailbox_row(const Mailbox& mb, const StateArgs& 
     // done, since a box's observables may flag the status.
     __shared__ double sh[3 * 32];
     __shared__ int last;
-    pending_observables(s, blockIdx.x, nb, sh);
+    pending_observables_all(s, blockIdx.x, nb, sh);
     const int wb = mb.sc_nwords / nb;
     for (int k = threadIdx.x; k < wb; k += blockDim.x) mb.sc_out[blockIdx.x * wb + k] = mb.sc[blockIdx.x * wb + k];
     if (nb > 1) {

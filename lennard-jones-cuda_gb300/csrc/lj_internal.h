@@ -70,14 +70,16 @@ struct DevScalars {
   int rec_cap;
   long long rec_count;
   // Fused steps compute a step's observables late (inside the next step's
-  // pair kernel, or in k_obs_finalize): obs_pending is the step mode
-  // (MODE_EVN / MODE_TVN) of a box whose K/V/W block partials are written
-  // but not yet summed, 0 if none; obs_slot is the first of the three
-  // block-partial slots that hold them; Tkin_rec is the Tkin of that step
-  // for its record.
-  double Tkin_rec;
-  int obs_pending;
-  int obs_slot;
+  // pair kernel, or in the read-back / k_obs_finalize), one entry per step
+  // parity: obs_pending[p] is the step mode (MODE_EVN / MODE_TVN) of a box
+  // whose K/V/W block partials from the step of parity p are written but not
+  // yet summed, 0 if none; obs_slot[p] is the first of the three
+  // block-partial slots that hold them; Tkin_rec[p] is the Tkin of that step
+  // for its record.  A step marks its own parity's entry and the next step's
+  // pair kernel consumes it, so the two never touch the same entry at once.
+  double Tkin_rec[2];
+  int obs_pending[2];
+  int obs_slot[2];
 };
 
 // Observable record layout written by the device (matches lj_observables).

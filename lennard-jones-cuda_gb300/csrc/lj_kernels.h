@@ -89,7 +89,7 @@ struct StateArgs {
   int* status;
   int4* q_next;                // fused step: predictor shadow for the next step
   int* blk_cnt;                // fused step: segments finished per i-block
-  int* glob_cnt;               // fused step: [2 + parity] pending-observables tickets, [4 + box] blocks finished
+  int* glob_cnt;               // fused step: [2 + parity] pending-observables tickets
   int nblocks;                 // i-blocks of all boxes
   int nsys;                    // boxes
   int obs_slot;                // fused EVN: first block-partial slot of this step's K, V, W (0 or 4, by parity)

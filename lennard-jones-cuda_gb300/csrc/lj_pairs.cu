@@ -217,7 +217,19 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
 
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
-  if (EPI && g == 0 && tid == 0) st.glob_cnt[st.ticket ^ 1] = 0;  // the other parity's ticket counter
+  if (EPI && g == 0) {
+    if (tid == 0) st.glob_cnt[st.ticket ^ 1] = 0;  // the other parity's ticket counter
+    if (EPI == MODE_EVN) {
+      // This step's observables are pending once the launch completes: its
+      // parity's entry is read only after that (the next step's pair kernel,
+      // a read-back), and this launch reads only the other parity's.
+      const int par = st.ticket - 2;
+      for (int sys = tid; sys < st.nsys; sys += THREADS) {
+        st.sc[sys].obs_slot[par] = st.obs_slot;
+        st.sc[sys].obs_pending[par] = MODE_EVN;
+      }
+    }
+  }
   // This CTA's j range: from offset lo0 of its first tile to offset lo1 of
   // tile t1 (lo1 = 0: up to the end of tile t1 - 1).
   const int t0 = a.cta_tile_begin[g], t1 = a.cta_tile_begin[g + 1];
@@ -428,32 +440,10 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
           __threadfence();
           fused_block_step<EPI>(st, B, shd);
           __syncthreads();
-          if (EPI == MODE_TVN) {
-            // chi is formed by k_tvn_close from the blocks' sums
-            if (tid == 0) st.blk_cnt[B] = 0;
-          } else {
-            // Last block of its box?  That CTA marks the box's observables
-            // pending (summed later by pending_observables).  Boxes finish
-            // independently, so a batch of many boxes has no serial stage at
-            // the end of the grid.
-            const int sys = bi.sys;
-            if (tid == 0) {
-              st.blk_cnt[B] = 0;
-              __threadfence();
-              const int nb_box = st.sys_block_first[sys + 1] - st.sys_block_first[sys];
-              sflag = (atomicAdd(st.glob_cnt + 4 + sys, 1) == nb_box - 1);
-            }
-            __syncthreads();
-            if (sflag) {
-              __threadfence();
-              if (tid == 0) {
-                st.sc[sys].obs_slot = st.obs_slot;
-                st.sc[sys].obs_pending = MODE_EVN;
-                st.glob_cnt[4 + sys] = 0;
-              }
-            }
-            __syncthreads();
-          }
+          // No per-box stage here: TVN's chi is formed by k_tvn_close from
+          // the blocks' sums, and EVN's observables were marked pending at
+          // the launch's start.
+          if (tid == 0) st.blk_cnt[B] = 0;
         }
       }
       if (block_end && !last) {
@@ -481,7 +471,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     __syncthreads();
     if (tid == 0) ticket = atomicAdd(st.glob_cnt + st.ticket, 1);
     __syncthreads();
-    if (ticket < st.nsys && !sfail) pending_observables(st, ticket, gridDim.x, shd);
+    if (ticket < st.nsys && !sfail) pending_observables(st, (st.ticket - 2) ^ 1, ticket, gridDim.x, shd);
     // The dependent kernel of a fused TVN step (k_tvn_close) may be scheduled
     // from here on; it waits for this grid's completion before reading.
     if (EPI == MODE_TVN) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

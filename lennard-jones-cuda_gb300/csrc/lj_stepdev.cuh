@@ -117,8 +117,11 @@ __device__ __forceinline__ void box_sum3(const StateArgs& s, int b0, int b1, dou
 // CalculateParameters (MDSystem.cpp:325-359) for box `sys`, plus t += dt for
 // steps (MDSystem.cpp:582) and the optional per-step record.  Block-wide call;
 // thread 0 writes.  sh: 3 x 32 doubles.
+// rec_parity >= 0: the record's Tkin is Tkin_rec[rec_parity] (TVN steps
+// whose observables were left pending), else the box's Tkin.
 template <int MODE>
-__device__ __forceinline__ void observables_box(const StateArgs& s, int sys, double* sh, int slot = 0) {
+__device__ __forceinline__ void observables_box(const StateArgs& s, int sys, double* sh, int slot = 0,
+                                                int rec_parity = -1) {
   const BoxArgs box = s.boxes[sys];
   const int b0 = s.sys_block_first[sys], b1 = s.sys_block_first[sys + 1];
   double kvw[3];
@@ -156,7 +159,7 @@ __device__ __forceinline__ void observables_box(const StateArgs& s, int sys, dou
     r.U = U;
     r.W = W;
     r.Pshear = sc.Pshear;
-    r.Tkin = MODE == MODE_TVN ? sc.Tkin_rec : sc.Tkin;
+    r.Tkin = (MODE == MODE_TVN && rec_parity >= 0) ? sc.Tkin_rec[rec_parity] : sc.Tkin;
     r.av_U = sc.av_U;
     r.av_T = sc.av_T;
     r.av_p = sc.av_p;
@@ -166,23 +169,35 @@ __device__ __forceinline__ void observables_box(const StateArgs& s, int sys, dou
   }
 }
 
-// Observables of the boxes whose fused step left them pending (block
-// partials K, V, W from k_tvn_close or the EVN epilogues, at obs_slot).
-// Called with a ticket from 0 .. tickets-1; ticket k takes boxes k,
-// k + tickets, ...  Block-wide call.
-static __device__ __noinline__ void pending_observables(const StateArgs& s, int ticket, int tickets, double* sh) {
+// Observables of the boxes whose fused step of parity `parity` left them
+// pending (block partials K, V, W from k_tvn_close or the EVN epilogues, at
+// obs_slot[parity]).  Called with a ticket from 0 .. tickets-1; ticket k
+// takes boxes k, k + tickets, ...  Block-wide call.
+static __device__ __noinline__ void pending_observables(const StateArgs& s, int parity, int ticket, int tickets,
+                                                        double* sh) {
   __shared__ int pend, slot;
   for (int sys = ticket; sys < s.nsys; sys += tickets) {
     if (threadIdx.x == 0) {
-      pend = s.sc[sys].obs_pending;
-      slot = s.sc[sys].obs_slot;
+      pend = s.sc[sys].obs_pending[parity];
+      slot = s.sc[sys].obs_slot[parity];
     }
     __syncthreads();
-    if (pend == MODE_TVN) observables_box<MODE_TVN>(s, sys, sh, slot);
+    if (pend == MODE_TVN) observables_box<MODE_TVN>(s, sys, sh, slot, parity);
     else if (pend == MODE_EVN) observables_box<MODE_EVN>(s, sys, sh, slot);
-    if (pend && threadIdx.x == 0) s.sc[sys].obs_pending = 0;
+    if (pend && threadIdx.x == 0) s.sc[sys].obs_pending[parity] = 0;
     __syncthreads();
   }
+}
+
+// Everything still pending, the older step first: the step before the last
+// fused one has parity s.ticket - 2 (the current parity), the last one the
+// other.  Normally only the last is left; the next step's pair kernel
+// consumes the one before it.
+static __device__ __forceinline__ void pending_observables_all(const StateArgs& s, int ticket, int tickets,
+                                                               double* sh) {
+  const int q = s.ticket - 2;
+  pending_observables(s, q, ticket, tickets, sh);
+  pending_observables(s, q ^ 1, ticket, tickets, sh);
 }
 
 // Sum of a particle's pair-kernel segments (5 values each).  The partials are

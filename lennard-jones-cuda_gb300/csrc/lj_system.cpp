@@ -471,7 +471,7 @@ lj_status build_and_swap_schedule(lj_system* s) {
   LJ_CUDA(s, sbf.alloc(s->nsys + 1));
   LJ_CUDA(s, bpart.alloc((size_t)nb * 8));
   LJ_CUDA(s, bcnt.alloc(nb));
-  LJ_CUDA(s, gcnt.alloc(4 + (size_t)s->nsys));
+  LJ_CUDA(s, gcnt.alloc(4));
   // partial: nseg x 5 x BI values of 8 bytes (FP64) or 4 bytes (MIXED)
   const size_t vals = (size_t)sch.nseg * 5 * threads;
   LJ_CUDA(s, partial.alloc(vals * (s->prec == LJ_PREC_FP64 ? 2 : 1)));
