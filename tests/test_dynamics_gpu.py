@@ -372,6 +372,47 @@ def test_step_io_matches_separate_calls(ljgb_mod, boundary):
         s.close()
 
 
+def test_read_back_waits_for_its_own_launch(ljgb_mod):
+    """A read-back into page-locked buffers waits on a completion word its
+    launch writes after its last store.  Behind a long run of steps (here
+    ~30 ms, past the word's 20 ms limit) the wait falls back to a stream
+    synchronisation; a new handle whose page-locked mirrors come from memory
+    an earlier handle used must not see that handle's words.  Both give what
+    separate calls give, bit for bit."""
+    n = 16384
+    kw = dict(n=n, density=0.85, temperature=1.0, canonical=1, lattice=ljgb_mod.LATTICE_FCC, jitter=0.02, seed=4)
+    a, b = ljgb_mod.System(**kw), ljgb_mod.System(**kw)
+    pa, va = ljgb_mod.pinned((n, 3)), ljgb_mod.pinned((n, 3))
+    a.get_state_into(pa, va, None)
+    oa = a.step_io(0.005, 150, pa, va, pa, va)
+    b.integrate(0.005, 150)
+    pb, vb, _ = b.get_state()
+    ob = b.observables()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    assert oa["U"] == ob["U"] and oa["step"] == ob["step"] == 150
+    # short calls: the completion word itself
+    for _ in range(3):
+        oa = a.step_io(0.005, 1, pa, va, pa, va)
+        b.integrate(0.005, 1)
+        ob = b.get_state_observables_into(pb, vb, None)
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb) and oa["U"] == ob["U"]
+    a.close()
+    b.close()
+    # fresh handles, created and read one after another
+    small = dict(n=700, density=0.6, temperature=1.1, canonical=0, lattice=ljgb_mod.LATTICE_FCC, jitter=0.02)
+    for seed in range(4):
+        c = ljgb_mod.System(seed=seed, **small)
+        c.integrate(0.005, 3)
+        oc = c.observables()
+        d = ljgb_mod.System(seed=seed, **small)
+        d.integrate(0.005, 3)
+        d.sync()
+        od = d.observables()
+        assert oc["U"] == od["U"] and oc["step"] == od["step"] == 3, seed
+        c.close()
+        d.close()
+
+
 def test_upload_writes_the_predictor(ljgb_mod):
     """On periodic boxes the upload's commit also writes the fused step's
     predictor, so the step after an upload launches no predictor kernel; a
