@@ -471,7 +471,7 @@ __device__ __forceinline__ void pairs_body(const PairArgs& a, const StateArgs& s
     __syncthreads();
     if (tid == 0) ticket = atomicAdd(st.glob_cnt + st.ticket, 1);
     __syncthreads();
-    if (ticket < st.nsys && !sfail) pending_observables(st, (st.ticket - 2) ^ 1, ticket, gridDim.x, shd);
+    if (ticket < st.nsys && !sfail) pending_observables(st, ticket, gridDim.x, shd);
     // The dependent kernel of a fused TVN step (k_tvn_close) may be scheduled
     // from here on; it waits for this grid's completion before reading.
     if (EPI == MODE_TVN) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

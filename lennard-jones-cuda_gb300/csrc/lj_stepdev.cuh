@@ -173,8 +173,8 @@ __device__ __forceinline__ void observables_box(const StateArgs& s, int sys, dou
 // pending (block partials K, V, W from k_tvn_close or the EVN epilogues, at
 // obs_slot[parity]).  Called with a ticket from 0 .. tickets-1; ticket k
 // takes boxes k, k + tickets, ...  Block-wide call.
-static __device__ __noinline__ void pending_observables(const StateArgs& s, int parity, int ticket, int tickets,
-                                                        double* sh) {
+__device__ __forceinline__ void pending_observables_parity(const StateArgs& s, int parity, int ticket, int tickets,
+                                                           double* sh) {
   __shared__ int pend, slot;
   for (int sys = ticket; sys < s.nsys; sys += tickets) {
     if (threadIdx.x == 0) {
@@ -189,15 +189,20 @@ static __device__ __noinline__ void pending_observables(const StateArgs& s, int 
   }
 }
 
+// In a fused step's pair kernel: the previous step's (the other parity's).
+static __device__ __noinline__ void pending_observables(const StateArgs& s, int ticket, int tickets, double* sh) {
+  pending_observables_parity(s, (s.ticket - 2) ^ 1, ticket, tickets, sh);
+}
+
 // Everything still pending, the older step first: the step before the last
 // fused one has parity s.ticket - 2 (the current parity), the last one the
 // other.  Normally only the last is left; the next step's pair kernel
 // consumes the one before it.
-static __device__ __forceinline__ void pending_observables_all(const StateArgs& s, int ticket, int tickets,
-                                                               double* sh) {
+static __device__ __noinline__ void pending_observables_all(const StateArgs& s, int ticket, int tickets,
+                                                            double* sh) {
   const int q = s.ticket - 2;
-  pending_observables(s, q, ticket, tickets, sh);
-  pending_observables(s, q ^ 1, ticket, tickets, sh);
+  pending_observables_parity(s, q, ticket, tickets, sh);
+  pending_observables_parity(s, q ^ 1, ticket, tickets, sh);
 }
 
 // Sum of a particle's pair-kernel segments (5 values each).  The partials are
