@@ -696,7 +696,7 @@ cudaError_t occupancy_fp64_t(int* blocks_per_sm) {
   X(1, 128, 512, 3, 6)  \
   X(2, 256, 256, 3, 3)  \
   X(3, 256, 512, 3, 3)  \
-  X(4, 256, 256, 3, 2)  \
+  X(4, 384, 512, 3, 2)  \
   X(5, 64, 256, 3, 12)
 
 const PairShape kShapes[] = {
