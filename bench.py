@@ -334,6 +334,7 @@ def extra_configs(torch, ljgb, oracle, dev, flush, peak):
     g = ljgb.System(n=n, density=1.1, temperature=1.0, canonical=1, lattice=ljgb.LATTICE_FCC, jitter=0.01,
                     seed=262144, device=dev, autotune=0)
     pos, _, F = g.get_state()
+    g.autotune()  # as the main configuration does (a few seconds at this size)
     i0 = int(np.random.default_rng(4096).integers(0, n - 4096))
     r = oracle.f64_forces(pos, g.L, True, rows=(i0, i0 + 4096))
     d = np.linalg.norm(F[i0:i0 + 4096] - r["F"], axis=1)
@@ -346,9 +347,11 @@ def extra_configs(torch, ljgb, oracle, dev, flush, peak):
     prof = g.profile_read()
     g.profile(False)
     pair_ms = prof["pair_ms"] / max(1, prof["pair_launches"])
+    tune = g.tune_info()
     g.close()
     out["large_262144"] = {
         "workload": "N=262144 rho*=1.1 T*=1.0 FCC+0.01 dt=0.004 TVN", "ms_per_step": ms / steps,
+        "kernel_shape": tune["shapes"][tune["active"]],
         "pair_interactions_per_s": n * (n - 1) * steps / (ms * 1e-3), "pair_kernel_ms": pair_ms,
         "fp32_frac": FLOPS_PER_PAIR * n * (n - 1) / (pair_ms * 1e-3) / 1e12 / peak,
         "subset_vs_fp64_oracle": {"rows": [i0, i0 + 4096], "gate_max": float((d / np.maximum(mag, rms)).max()),
