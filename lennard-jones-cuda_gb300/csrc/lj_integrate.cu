@@ -401,7 +401,23 @@ __global__ void k_tvn_close(StateArgs s) {
   // order (as k_tvn_finish does), so no CTA of the pair kernel has to wait
   // for the box's last block to compute it.
   __shared__ double chi_sh, tkin_sh;
-  {
+  if (b1 - b0 <= 32) {
+    // Boxes of at most 32 blocks (batches of small boxes): warp 0 alone.
+    // box_sum would give every block value to one thread of warp 0 and zeros
+    // to the other warps, then add 0 + w0 + 0 + ...: the same bits as
+    // 0 + w0, with a quarter of the FP64 work (this kernel is FP64-bound on
+    // batches).
+    if (tid < 32) {
+      double v = b0 + tid < b1 ? __ldcg(s.blk_part + (size_t)(b0 + tid) * 8 + 3) : 0.0;
+      v = warp_sum(v);
+      if (tid == 0) {
+        double Tkin;
+        chi_sh = tvn_chi(box, 0.0 + v, &Tkin);
+        tkin_sh = Tkin;
+      }
+    }
+    __syncthreads();
+  } else {
     const double tv2 = box_sum(s, b0, b1, 3, sh);
     if (tid == 0) {
       double Tkin;
