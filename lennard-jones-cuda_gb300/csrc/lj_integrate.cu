@@ -359,10 +359,10 @@ __global__ void k_predict(StateArgs s) {
 // tF = F_n/2 + F_{n+1}/2, v = (2 chi - 1) v + chi dt tF, boundaries,
 // F <- F_{n+1}, the next step's predictor, and block partials K, V, W.
 // The observables of the step (sums over blocks, averages, record) are left
-// pending: the next step's pair kernel computes them in a CTA that has
-// finished its pair work (pending_observables), or k_obs_finalize does
-// before the host reads them.  This takes a serial last-CTA stage off the
-// step's critical path.
+// pending in this step's parity entry: the next step's pair kernel computes
+// them in a CTA that has finished its pair work (pending_observables), or
+// the read-back launch / k_obs_finalize does before the host reads them.
+// This takes a serial last-CTA stage off the step's critical path.
 __global__ void k_tvn_close(StateArgs s) {
   __shared__ double sh[3 * 32];
   // Launched as a programmatic dependent of the pair kernel: the CTAs start
@@ -471,7 +471,8 @@ __global__ void k_tvn_close(StateArgs s) {
   }
 }
 
-// Observables left pending by the last fused TVN step (one CTA per box).
+// Observables left pending by the last fused steps, EVN or TVN (one CTA per
+// box).
 __global__ void k_obs_finalize(StateArgs s) {
   __shared__ double sh[3 * 32];
   pending_observables_all(s, blockIdx.x, gridDim.x, sh);

@@ -757,10 +757,11 @@ lj_status get_graph(lj_system* s, int mode, GraphEntry** out) {
   return LJ_OK;
 }
 
-// Computes the observables that fused TVN steps left pending
-// (k_obs_finalize; boxes whose observables a later pair kernel already
-// computed are skipped on the device).  Called before anything reads or
-// changes the observables, the running sums or the block partials.
+// Computes the observables that fused steps left pending (k_obs_finalize;
+// entries a later pair kernel already consumed are skipped on the device).
+// Called before anything reads or changes the observables, the running sums
+// or the block partials; a read-back that returns the observables computes
+// them in its own launch instead.
 lj_status flush_observables(lj_system* s) {
   if (!s->obs_maybe_pending) return LJ_OK;
   s->obs_maybe_pending = false;
