@@ -110,7 +110,8 @@ def test_initial_speeds_are_maxwellian(ljlib):
 @pytest.mark.parametrize("n,block,tile,ctas", [
     ([16384], 128, 256, 1216), ([16384], 128, 256, 1824), ([400], 128, 256, 1824),
     ([1000, 37, 4000, 200], 64, 256, 608), ([5], 128, 256, 1824), ([262144], 128, 256, 1824),
-    ([777], 256, 512, 300), ([1000, 37, 4000, 200], 128, 512, 2000)])
+    ([777], 256, 512, 300), ([1000, 37, 4000, 200], 128, 512, 2000),
+    ([16384], 384, 512, 304), ([262144], 384, 512, 304), ([1000, 37, 4000, 200], 384, 512, 304)])
 def test_schedule_covers_every_pair_once(ljlib, n, block, tile, ctas):
     """Every (i-block, j) belongs to exactly one CTA, CTA ranges are cut on
     32-record chunks, each (CTA, block) pair has its own segment in the
