@@ -245,6 +245,37 @@ def test_fused_matches_unfused_path(ljgb_mod, boundary):
             assert p0[7, 0] < L + 0.3 + 0.1 and v0[7, 0] < 0    # turned back by the wall at x = L
 
 
+@pytest.mark.parametrize("shape", range(6))
+def test_fused_step_every_shape(ljgb_mod, shape):
+    """Every pair-kernel shape (i-blocks of 64 to 384 particles, ragged last
+    blocks) runs the fused step -- block epilogues, per-parity pending
+    observables, TVN chi in the close kernel -- as the FP64 path steps the same
+    box, periodic and walled, in both ensembles."""
+    N, rho = 3001, 0.8
+    pos, vel, L = U.lattice_state(N, rho, 1.1, "fcc", 0.02, seed=31)
+    for boundary in (0, 1):
+        for canonical in (0, 1):
+            out = []
+            for prec in (0, 1):
+                s = ljgb_mod.System(n=N, density=rho, temperature=1.0, canonical=canonical, precision=prec,
+                                    boundary=boundary)
+                if prec == 0:
+                    s.set_kernel_shape(shape)
+                s.set_state(pos, vel)
+                s.calculate_forces()
+                s.integrate(0.004, 7)
+                s.integrate(0.004, 8)
+                out.append((s.get_state(), s.observables()))
+                s.close()
+            (p0, v0, _), o0 = out[0]
+            (p1, v1, _), o1 = out[1]
+            assert np.abs(p0 - p1).max() < 1e-6 * L, (boundary, canonical)
+            assert np.abs(v0 - v1).max() < 1e-5, (boundary, canonical)
+            for k in ("K", "V", "T", "P", "U", "t"):
+                assert o0[k] == pytest.approx(o1[k], rel=1e-6, abs=1e-6), (boundary, canonical, k)
+            assert o0["step"] == o1["step"] == 15 and o0["av_iters"] == o1["av_iters"] == 16
+
+
 def test_autotune_keeps_the_state(ljgb_mod):
     s = ljgb_mod.System(n=2000, density=0.85, temperature=1.0, canonical=1, lattice=1, jitter=0.02)
     s.set_recording(8)
