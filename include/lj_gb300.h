@@ -229,7 +229,9 @@ float lj_reference_rdf_dr2(int32_t n);
 lj_status lj_velocity_counts(lj_system* sys, double step, int32_t nbins, uint64_t* counts);
 
 /* Selects the pair-kernel shape by index (see lj_tune_info) or -1 for the
- * autotuned choice; lj_autotune times every shape now and keeps the fastest. */
+ * autotuned choice; lj_autotune times every shape now and keeps the fastest.
+ * Changing the shape (or the split cap below) recomputes the forces for the
+ * next step; the observables, the clock and the running averages are kept. */
 lj_status lj_autotune(lj_system* sys);
 lj_status lj_set_kernel_shape(lj_system* sys, int32_t shape);
 /* Shape table: count, and for shape k its threads per CTA, i-particles per

@@ -957,6 +957,18 @@ lj_status write_scalars(lj_system* s, const std::vector<DevScalars>& in) {
   return LJ_OK;
 }
 
+// A new schedule changes only how the pair sums are cut and rounded: the
+// forces are recomputed for the next step, while the observables, the clock
+// and the running averages stay as they were (the state did not change, so
+// the recomputation is no new sample of the averages).
+lj_status recompute_forces_keep_scalars(lj_system* s) {
+  std::vector<DevScalars> sc;
+  lj_status st = read_scalars(s, sc);
+  if (st) return st;
+  if ((st = enqueue_compute_forces(s))) return st;
+  return write_scalars(s, sc);
+}
+
 void fill_obs(const DevScalars& d, lj_observables* o) {
   o->t = d.t;
   o->K = d.K;
@@ -1923,7 +1935,7 @@ lj_status lj_set_kernel_shape(lj_system* s, int32_t shape) {
     return st;
   }
   // The i-block length changed: rebuild shadows and the per-block sums.
-  return enqueue_compute_forces(s);
+  return recompute_forces_keep_scalars(s);
 }
 
 lj_status lj_set_split_cap(lj_system* s, int32_t cap) {
@@ -1940,7 +1952,7 @@ lj_status lj_set_split_cap(lj_system* s, int32_t cap) {
     return st;
   }
   // The partial segments were re-cut: rebuild the per-block sums.
-  return enqueue_compute_forces(s);
+  return recompute_forces_keep_scalars(s);
 }
 
 lj_status lj_split_info(lj_system* s, int32_t* cap, int32_t* ctas, int32_t* max_segments) {
